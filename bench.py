@@ -1,0 +1,382 @@
+"""Benchmark of the GB300 sparse-mesh path; prints one JSON line.
+
+Workloads (``--workload``):
+  swe      shallow water on the tutorial mesh, N=2000 (16,000,000 cells,
+           47,992,000 directed edges), centred Gaussian bump, dt=5e-4; one
+           bench step = one time step (4 fused stage kernels); metric
+           cell-steps/s.  Default dtype f32 (``--dtype f64`` for FP64).
+  poisson  P1 Poisson, 1000x1000 grid (998,001 unknowns, 5,980,016 directed
+           couplings), random-mode RHS, Jacobi-PCG to relative residual 1e-8;
+           one bench step = one solve; metric solves/s
+           (``--precision native|mixed``).
+
+``--impl reference`` times the oracle (the reference's CPU algorithm, the
+same aten ops its CPU backend runs) on this machine's host cores, on a
+bounded sample of the same workload.  Under torchrun (N>1) every rank runs
+an independent replica (the path does not shard at world size 1); the
+printed value is all ranks' work over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def _max_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ SWE --
+def swe_cpu_baseline(n, dtype, dt, steps):
+    """Oracle SWE step on the host cores; returns (cell-steps/s, threads)."""
+    from easier_gb300 import mesh
+    from oracle import swe as oswe
+    m = mesh.triangular_mesh(n)
+    g = mesh.swe_geometry(m)
+    p = oswe.SweProblem(m.src, m.dst, m.bcells, g.sx, g.sy, g.alpha, g.bsx, g.bsy, g.area, dt, dtype)
+    h = torch.from_numpy(mesh.gaussian_bump(g.x, g.y)).to(dtype)
+    uh = torch.zeros_like(h)
+    vh = torch.zeros_like(h)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h, uh, vh = p.step(h, uh, vh)
+    wall = time.perf_counter() - t0
+    return m.nc * steps / wall, torch.get_num_threads(), wall
+
+
+def bench_swe(args, world, rank, local):
+    import ctypes
+
+    import easier_gb300 as esr
+    from easier_gb300 import _lib, workloads
+    dtype = torch.float32 if args.dtype == "f32" else torch.float64
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=dtype)
+    [eqn] = esr.compile([eqn], "cuda")
+    eng = eqn.easier_fused_engine
+    if eng is None:
+        raise RuntimeError("the fused shallow-water engine was not installed")
+    nc = eng.nc
+    stream = torch.cuda.current_stream(dev)
+    eng.step(args.warmup)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        _barrier(world)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        eng.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        _barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms_max = _max_over_ranks(world, ms)
+    h = eqn.h.collect()
+    if not bool(torch.isfinite(h).all()):
+        raise RuntimeError("non-finite shallow-water state after the timed steps")
+    value = world * nc * args.steps / (ms_max / 1e3)
+    bytes_step = eng.workload_bytes_per_step()
+    peak, peak_kind = _peaks()
+    achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
+
+    # end to end through the C ABI with host buffers: every step uploads the
+    # packed state from pinned host memory, runs esr_swe_step, reads it back
+    host = torch.empty((nc, 4), dtype=dtype, pin_memory=True)
+    host.copy_(eng.state)
+    ke = max(1, min(args.steps, args.e2e_steps))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(ke):
+        eng.state.copy_(host, non_blocking=True)
+        _lib.call("esr_swe_step", ctypes.byref(eng._mesh), float(args.dt), _lib.ptr(eng.state), 1,
+                  _lib.ptr(eng.ws), stream.cuda_stream)
+        host.copy_(eng.state, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_wall = time.perf_counter() - t0
+    e2e_ms = _max_over_ranks(world, max(e2e_ms, e2e_wall * 1e3))
+    e2e = {"value": world * nc * ke / (e2e_ms / 1e3), "unit": "cell-steps/s",
+           "h2d_bytes_per_step": host.numel() * host.element_size(),
+           "d2h_bytes_per_step": host.numel() * host.element_size(), "steps": ke,
+           "path": "esr_swe_step via ctypes, state [nc,4] from/to pinned host memory each step"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, thr, wall = swe_cpu_baseline(args.n, dtype, args.dt, args.cpu_steps)
+        cpu = {"value": v, "unit": "cell-steps/s", "cores": thr, "kind": "port",
+               "sample": f"{args.cpu_steps} oracle steps (torch CPU ops, reference op order) at N={args.n}, "
+                         f"{args.dtype}, {wall:.1f} s"}
+    traffic = _ncu_traffic("swe", args)
+    line = {
+        "metric": "SWE cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic (tutorial mesh generator, centred Gaussian bump, uh=vh=0)",
+        "config": {"workload": f"shallow water, tutorial mesh N={args.n} ({nc} cells, {eng.b['ne']} directed edges), "
+                               f"RCM + destination-ordered face slots, dt={args.dt}",
+                   "cells": nc, "edges": eng.b["ne"], "dt": args.dt, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (state+geometry ~%.2f GB)" % (bytes_step / 4 / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "kernel": "swe_stage_kernel (4 launches per step; bytes and time per step / 4)",
+                     "algorithmic_bytes_per_launch": bytes_step / 4},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * args.steps, "clocks": clk.summary(),
+    }
+    return line
+
+
+def _ncu_traffic(kind, args):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    d = json.loads(f.read_text())
+    key = f"{kind}_{args.dtype}"
+    return d.get(key)
+
+
+# -------------------------------------------------------------- Poisson --
+def bench_poisson(args, world, rank, local):
+    import easier_gb300 as esr
+    from easier_gb300 import workloads
+    from easier_gb300.numeric.preconditioner import Jacobi
+    from easier_gb300.numeric.solver import CG
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    eqn = workloads.P1Poisson(args.n, rhs_seed=0)
+    sol = CG(eqn.A, eqn.b, eqn.x, M=Jacobi(eqn.A))
+    [eqn, sol] = esr.compile([eqn, sol], "cuda")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        eqn.x.data.zero_()
+        sol.solve(rtol=1e-8, precision=args.precision)
+    torch.cuda.synchronize(dev)
+    iters = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        _barrier(world)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            eqn.x.data.zero_()
+            info = sol.solve(rtol=1e-8, precision=args.precision)
+            iters.append(info["iters"])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        _barrier(world)
+    ms = _max_over_ranks(world, e0.elapsed_time(e1))
+    bnorm = float(torch.linalg.vector_norm(eqn.b.data))
+    rel = info["true_residual"] / bnorm
+    if not rel <= 1e-8 * 1.0001:
+        raise RuntimeError(f"true relative residual {rel:.3e} above 1e-8")
+    nit = statistics.mean(iters)
+    eng = sol._fused
+    A = eng.A if hasattr(eng, "A") else eng.A64
+    s = A.val.element_size()
+    bytes_it = A.col.numel() * (4 + s) + A.n * (8 + 2 * s) + A.n * 12 * s
+    achieved = bytes_it * nit / (ms / args.steps / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    line = {
+        "metric": "Poisson solves/s", "value": world * args.steps / (ms / 1e3), "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "native" else "f32-spmv/f64-dot",
+        "data": "synthetic (16 random sine modes, seed 0)",
+        "config": {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to FP64 true rel. residual 1e-8",
+                   "unknowns": A.n, "couplings": int(A.nnz), "iterations": nit, "precision": args.precision,
+                   "true_rel_residual": rel, "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None},
+        "gpu_launches": int(eng.kernel_launches if hasattr(eng, "kernel_launches") else 0),
+        "clocks": clk.summary(),
+    }
+    return line
+
+
+# ------------------------------------------------------------ reference --
+def bench_reference(args):
+    """The reference's CPU algorithm (oracle) on the host cores."""
+    torch.set_num_threads(os.cpu_count() or 1)
+    if args.workload == "swe":
+        dtype = torch.float32 if args.dtype == "f32" else torch.float64
+        from easier_gb300 import mesh
+        from oracle import swe as oswe
+        m = mesh.triangular_mesh(args.n)
+        g = mesh.swe_geometry(m)
+        p = oswe.SweProblem(m.src, m.dst, m.bcells, g.sx, g.sy, g.alpha, g.bsx, g.bsy, g.area, args.dt, dtype)
+        h = torch.from_numpy(mesh.gaussian_bump(g.x, g.y)).to(dtype)
+        uh, vh = torch.zeros_like(h), torch.zeros_like(h)
+        for _ in range(args.warmup):
+            h, uh, vh = p.step(h, uh, vh)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            h, uh, vh = p.step(h, uh, vh)
+        wall = time.perf_counter() - t0
+        v = m.nc * args.steps / wall
+        unit, metric = "cell-steps/s", "SWE cell-steps/s"
+        sample = f"{args.steps} full oracle steps at N={args.n} ({m.nc} cells), {args.dtype}"
+        cfg = {"workload": f"shallow water, tutorial mesh N={args.n} ({m.nc} cells, {m.ne} directed edges), dt={args.dt}"}
+    else:
+        from easier_gb300 import mesh
+        from oracle import cg as ocg
+        s = mesh.p1_system(args.n)
+        b = mesh.random_mode_rhs(args.n, 0)
+        for _ in range(args.warmup):
+            ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-8, jacobi=True)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            x, it, _ = ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-8, jacobi=True)
+        wall = time.perf_counter() - t0
+        v = args.steps / wall
+        unit, metric = "solves/s", "Poisson solves/s"
+        sample = f"{args.steps} full Jacobi-PCG solves ({it} iterations each) on the {args.n}x{args.n} P1 grid"
+        cfg = {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to rel. residual 1e-8"}
+    cores = torch.get_num_threads()
+    return {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=None)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["swe", "poisson"], default="swe")
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--precision", choices=["native", "mixed"], default="native")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.n is None:
+        args.n = 2000 if args.workload == "swe" else 1000
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        if args.steps is None:
+            args.steps = 3 if args.workload == "swe" else 1
+        if args.warmup is None:
+            args.warmup = 1 if args.workload == "swe" else 0
+        if rank != 0:
+            return
+        print(json.dumps(bench_reference(args)), flush=True)
+        return
+    if args.steps is None:
+        args.steps = 1000 if args.workload == "swe" else 10
+    if args.warmup is None:
+        args.warmup = 10 if args.workload == "swe" else 3
+    if args.warmup < 3:
+        args.warmup = 3
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    line = bench_swe(args, world, rank, local) if args.workload == "swe" else bench_poisson(args, world, rank, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+"""Build recipe for the native library ``libesr_gb300.so``.
+
+Compiles every translation unit under ``easier_gb300/csrc`` in parallel:
+CUDA files with ``nvcc -gencode arch=compute_103a,code=sm_103a`` (GB300
+only), host C++ with ``g++ -O2 -ffp-contract=off`` (the assembly code must
+not contract a*b+c into an FMA, so its values match the reference's CPU run
+bit for bit on x86 and on aarch64).  Objects go to ``_build/`` beside the
+package, the library into the package directory (in-tree, git-ignored).
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+INCLUDE = ROOT / "include"
+BUILD = ROOT / "_build"
+LIB_NAME = "libesr_gb300.so"
+LIB_PATH = PKG / LIB_NAME
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build easier_gb300")
+    return cand
+
+
+def _sources():
+    cu = sorted(CSRC.glob("*.cu"))
+    cpp = sorted(CSRC.glob("*.cpp"))
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+    return cu, cpp, headers
+
+
+def _digest(files, extra: str) -> str:
+    h = hashlib.sha256(extra.encode())
+    for f in files:
+        h.update(f.name.encode())
+        h.update(f.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the library if any source changed; return its path."""
+    cu, cpp, headers = _sources()
+    nvcc = _nvcc()
+    flags_key = " ".join(ARCH + NVCC_FLAGS + CXX_FLAGS + [os.uname().machine])
+    digest = _digest(cu + cpp + headers, flags_key)
+    stamp = PKG / ".libesr_gb300.stamp"
+    if not force and LIB_PATH.exists() and stamp.exists() and stamp.read_text() == digest:
+        return LIB_PATH
+    BUILD.mkdir(exist_ok=True)
+
+    def compile_one(src: Path) -> Path:
+        obj = BUILD / (src.name + ".o")
+        if src.suffix == ".cu":
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        else:
+            cmd = ["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compiling {src.name} failed:\n{r.stdout}\n{r.stderr}")
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, cu + cpp))
+    tmp = LIB_PATH.with_suffix(".so.tmp")
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"linking {LIB_NAME} failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    stamp.write_text(digest)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,145 @@
+"""ctypes binding of ``libesr_gb300.so`` (declared in ``include/esr_gb300.h``).
+
+The library is loaded once per process.  If it is missing or was built from
+different sources, the import of any device op raises: there is no CPU
+fallback for the device path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from ctypes import POINTER, Structure, c_double, c_int, c_int32, c_int64, c_void_p, c_char_p
+from pathlib import Path
+
+from .utils import EasierJitException
+
+F32, F64, I32, I64 = 0, 1, 2, 3
+REDUCE_OPS = {"sum": 0, "prod": 1, "mean": 2, "amax": 3, "amin": 4}
+AGG_SUM, AGG_PROD, AGG_NORM, AGG_MAX, AGG_MIN = 0, 1, 2, 3, 4
+DEV_IDX_RANGE, DEV_NONFINITE = 1, 2
+
+_LOCK = threading.Lock()
+_LIB = None
+
+
+class SweMesh(Structure):
+    _fields_ = [("nc", c_int64), ("width", c_int32), ("dtype", c_int32),
+                ("nbr", c_void_p), ("sx", c_void_p), ("sy", c_void_p),
+                ("alpha", c_void_p), ("area", c_void_p)]
+
+
+class Sell(Structure):
+    _fields_ = [("n", c_int64), ("nslots", c_int64), ("dtype", c_int32), ("pad_", c_int32),
+                ("slice_ptr", c_void_p), ("col", c_void_p), ("val", c_void_p), ("diag", c_void_p)]
+
+
+class CgScalars(Structure):
+    _fields_ = [("rz", c_double), ("pq", c_double), ("alpha", c_double), ("beta", c_double),
+                ("rr", c_double), ("bnorm", c_double), ("tol", c_double), ("rz_new", c_double),
+                ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("pad_", c_int32)]
+
+
+_P = c_void_p
+_SIGS = {
+    "esr_last_error": (c_char_p, []),
+    "esr_abi_version": (c_int, []),
+    "esr_device_status": (c_int, [POINTER(c_int), c_int, _P]),
+    "esr_mesh_sizes": (c_int, [c_int64, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    "esr_mesh_triangular": (c_int, [c_int64, _P, _P, _P, _P, _P, _P]),
+    "esr_swe_geometry": (c_int, [c_int64, c_int64, c_int64] + [_P] * 14),
+    "esr_poisson_fv_assemble": (c_int, [c_int64, c_int64, c_int64] + [_P] * 11),
+    "esr_p1_sizes": (c_int, [c_int64, POINTER(c_int64), POINTER(c_int64)]),
+    "esr_p1_assemble": (c_int, [c_int64, _P, _P, _P, _P, _P]),
+    "esr_csr_from_index": (c_int, [_P, c_int64, c_int64, _P, _P]),
+    "esr_rcm_order": (c_int, [c_int64, c_int64, _P, _P, _P]),
+    "esr_sell_build": (c_int, [c_int64, _P, _P, _P, c_int64, _P, _P, _P]),
+    "esr_gather": (c_int, [_P, c_int64, c_int64, _P, c_int64, _P, _P]),
+    "esr_segreduce": (c_int, [c_int, c_int, _P, c_int64, _P, _P, c_int64, _P, _P]),
+    "esr_aggregate_workspace_bytes": (c_int64, [c_int64, c_int64]),
+    "esr_aggregate": (c_int, [c_int, c_int, _P, c_int64, c_int64, _P, _P, _P]),
+    "esr_dot_workspace_bytes": (c_int64, [c_int64]),
+    "esr_dot": (c_int, [c_int, _P, _P, c_int64, _P, _P, _P]),
+    "esr_swe_workspace_bytes": (c_int64, [POINTER(SweMesh)]),
+    "esr_swe_step": (c_int, [POINTER(SweMesh), c_double, _P, c_int64, _P, _P]),
+    "esr_swe_delta": (c_int, [POINTER(SweMesh), _P, _P, _P]),
+    "esr_spmv": (c_int, [POINTER(Sell), _P, _P, _P]),
+    "esr_cg_workspace_bytes": (c_int64, [c_int64]),
+    "esr_cg_init": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_double, c_double, c_int32, _P, _P]),
+    "esr_cg_iterate": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_int32, _P, _P]),
+    "esr_cg_read_scalars": (c_int, [_P, POINTER(CgScalars), _P]),
+    "esr_true_residual": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P]),
+    "esr_convert": (c_int, [c_int, _P, c_int, _P, c_int64, c_double, _P]),
+    "esr_axpy_f64": (c_int, [_P, c_int, _P, c_double, c_int64, _P]),
+}
+
+ABI_VERSION = 1
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "libesr_gb300.so"
+
+
+def lib():
+    """The loaded library; builds it first when it is absent or stale."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = library_path()
+        if os.environ.get("EASIER_GB300_NO_BUILD") != "1":
+            from . import _build
+            path = _build.build()
+        if not path.exists():
+            raise EasierJitException(
+                f"native library {path} is missing; run `python -c 'import __graft_entry__ as g; g.build()'`")
+        handle = ctypes.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        if handle.esr_abi_version() != ABI_VERSION:
+            raise EasierJitException("libesr_gb300.so ABI version mismatch; rebuild it")
+        _LIB = handle
+        return _LIB
+
+
+def exported_symbols():
+    return list(_SIGS.keys())
+
+
+def check(status: int, what: str = "") -> None:
+    """Raise on a non-zero status from the library."""
+    if status != 0:
+        msg = lib().esr_last_error()
+        msg = msg.decode() if msg else ""
+        kinds = {1: ValueError, 2: RuntimeError, 3: RuntimeError, 4: NotImplementedError}
+        raise kinds.get(status, RuntimeError)(f"{what}: {msg}" if what else msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args), name)
+
+
+def ptr(t) -> int:
+    """Device or host address of a torch tensor / numpy array (None -> NULL)."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def stream_handle(device=None) -> int:
+    import torch
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def dtype_code(dtype) -> int:
+    import torch
+    m = {torch.float32: F32, torch.float64: F64, torch.int32: I32, torch.int64: I64}
+    if dtype not in m:
+        raise NotImplementedError(f"dtype {dtype} is not supported by the GB300 path")
+    return m[dtype]

@@ -1,0 +1,218 @@
+// Host-side integer work: error reporting, CSR construction from a Reducer
+// index, and reverse Cuthill-McKee ordering.  All of it is exact integer
+// arithmetic and deterministic.
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "esr_internal.h"
+
+namespace {
+thread_local std::string t_last_error;
+}
+
+namespace esr {
+int fail(int code, const std::string &msg) {
+  t_last_error = msg;
+  return code;
+}
+}  // namespace esr
+
+extern "C" const char *esr_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" int esr_abi_version(void) { return ESR_GB300_ABI_VERSION; }
+
+// Stable counting sort: the edge order the reference's reorder pass gives a
+// Reducer at world size 1 (sparse_encoding.py:244-338 with the stable
+// zipsort of passes/utils.py:301-336), plus the CSR row pointer.
+extern "C" int esr_csr_from_index(const int64_t *idx, int64_t m, int64_t n,
+                                  int64_t *rowptr, int64_t *perm) {
+  if (m < 0 || n < 0) return esr::fail(ESR_ERR_ARG, "negative size");
+  if (!rowptr || (m && (!idx || !perm))) return esr::fail(ESR_ERR_ARG, "null pointer");
+  std::fill(rowptr, rowptr + n + 1, 0);
+  for (int64_t k = 0; k < m; ++k) {
+    int64_t v = idx[k];
+    if (v < 0 || v >= n)
+      return esr::fail(ESR_ERR_ARG, "index " + std::to_string(v) + " at position " +
+                                        std::to_string(k) + " is out of range [0, " +
+                                        std::to_string(n) + ")");
+    rowptr[v + 1] += 1;
+  }
+  for (int64_t i = 0; i < n; ++i) rowptr[i + 1] += rowptr[i];
+  std::vector<int64_t> fill(rowptr, rowptr + n);
+  for (int64_t k = 0; k < m; ++k) perm[fill[idx[k]]++] = k;
+  return ESR_OK;
+}
+
+// Reverse Cuthill-McKee.
+//  1. Build the undirected simple graph (both directions, no self loops,
+//     no duplicate neighbours); neighbour lists sorted by (degree, index).
+//  2. For each component, in order of its lowest-degree lowest-index
+//     unvisited vertex: find a pseudo-peripheral start by repeated BFS
+//     (move to the lowest-degree vertex of the last level while the
+//     eccentricity grows, at most 16 rounds), then Cuthill-McKee BFS.
+//  3. Reverse the concatenated order.
+extern "C" int esr_rcm_order(int64_t n, int64_t m, const int64_t *src,
+                             const int64_t *dst, int64_t *order) {
+  if (n < 0 || m < 0) return esr::fail(ESR_ERR_ARG, "negative size");
+  if (!order || (m && (!src || !dst))) return esr::fail(ESR_ERR_ARG, "null pointer");
+  if (n == 0) return ESR_OK;
+  for (int64_t e = 0; e < m; ++e)
+    if (src[e] < 0 || src[e] >= n || dst[e] < 0 || dst[e] >= n)
+      return esr::fail(ESR_ERR_ARG, "edge endpoint out of range");
+
+  // undirected adjacency in CSR
+  std::vector<int64_t> deg(n + 1, 0);
+  for (int64_t e = 0; e < m; ++e) {
+    if (src[e] == dst[e]) continue;
+    deg[src[e] + 1]++;
+    deg[dst[e] + 1]++;
+  }
+  for (int64_t i = 0; i < n; ++i) deg[i + 1] += deg[i];
+  std::vector<int64_t> adj(deg[n]);
+  {
+    std::vector<int64_t> pos(deg.begin(), deg.end() - 1);
+    for (int64_t e = 0; e < m; ++e) {
+      if (src[e] == dst[e]) continue;
+      adj[pos[src[e]]++] = dst[e];
+      adj[pos[dst[e]]++] = src[e];
+    }
+  }
+  // dedupe each list
+  std::vector<int64_t> ptr(n + 1, 0);
+  {
+    int64_t w = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t b = deg[i], e = deg[i + 1];
+      std::sort(adj.begin() + b, adj.begin() + e);
+      ptr[i] = w;
+      for (int64_t k = b; k < e; ++k)
+        if (k == b || adj[k] != adj[k - 1]) adj[w++] = adj[k];
+    }
+    ptr[n] = w;
+    adj.resize(w);
+  }
+  std::vector<int64_t> degree(n);
+  for (int64_t i = 0; i < n; ++i) degree[i] = ptr[i + 1] - ptr[i];
+  auto by_degree = [&](int64_t a, int64_t b) {
+    return degree[a] != degree[b] ? degree[a] < degree[b] : a < b;
+  };
+  for (int64_t i = 0; i < n; ++i) std::sort(adj.begin() + ptr[i], adj.begin() + ptr[i + 1], by_degree);
+
+  // candidate roots in (degree, index) order
+  std::vector<int64_t> roots(n);
+  for (int64_t i = 0; i < n; ++i) roots[i] = i;
+  std::stable_sort(roots.begin(), roots.end(), by_degree);
+
+  std::vector<int64_t> level(n, -1);  // scratch for the peripheral search
+  std::vector<int64_t> touched;
+  std::vector<char> placed(n, 0);
+  int64_t out = 0;
+
+  auto bfs_last_level = [&](int64_t s, int64_t &ecc) -> int64_t {
+    // BFS limited to s's component; returns the lowest (degree, index)
+    // vertex of the deepest level.
+    touched.clear();
+    std::vector<int64_t> q;
+    q.push_back(s);
+    level[s] = 0;
+    touched.push_back(s);
+    size_t h = 0;
+    int64_t maxl = 0;
+    while (h < q.size()) {
+      int64_t v = q[h++];
+      for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+        int64_t w = adj[k];
+        if (level[w] < 0) {
+          level[w] = level[v] + 1;
+          maxl = std::max(maxl, level[w]);
+          q.push_back(w);
+          touched.push_back(w);
+        }
+      }
+    }
+    int64_t best = -1;
+    for (int64_t v : q)
+      if (level[v] == maxl && (best < 0 || by_degree(v, best))) best = v;
+    for (int64_t v : touched) level[v] = -1;
+    ecc = maxl;
+    return best;
+  };
+
+  for (int64_t ri = 0; ri < n; ++ri) {
+    int64_t r = roots[ri];
+    if (placed[r]) continue;
+    // pseudo-peripheral vertex
+    int64_t start = r, ecc = 0;
+    int64_t cand = bfs_last_level(start, ecc);
+    for (int round = 0; round < 16; ++round) {
+      int64_t ecc2 = 0;
+      int64_t cand2 = bfs_last_level(cand, ecc2);
+      if (ecc2 <= ecc) break;
+      start = cand;
+      ecc = ecc2;
+      cand = cand2;
+    }
+    // Cuthill-McKee BFS
+    int64_t head = out;
+    order[out++] = start;
+    placed[start] = 1;
+    while (head < out) {
+      int64_t v = order[head++];
+      for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+        int64_t w = adj[k];
+        if (!placed[w]) {
+          placed[w] = 1;
+          order[out++] = w;
+        }
+      }
+    }
+  }
+  std::reverse(order, order + n);
+  return ESR_OK;
+}
+
+// SELL-32 layout of a Linsys.  Slices of 32 consecutive rows; a slice is as
+// wide as its longest row; entries stored slot-major so a warp reads one
+// slot of 32 rows contiguously.  Row entries keep the CSR (= reference edge)
+// order.
+extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *perm,
+                              const int64_t *colidx, int64_t ncols, int64_t *slice_ptr,
+                              int32_t *col, int64_t *src_pos) {
+  if (n < 0 || ncols < 0) return esr::fail(ESR_ERR_ARG, "negative size");
+  if (!rowptr || !slice_ptr) return esr::fail(ESR_ERR_ARG, "null pointer");
+  if (ncols > ((int64_t)1 << 31) - 1) return esr::fail(ESR_ERR_UNSUPPORTED, "more than 2^31-1 columns");
+  const int64_t nslices = (n + 31) / 32;
+  slice_ptr[0] = 0;
+  for (int64_t s = 0; s < nslices; ++s) {
+    int64_t w = 0;
+    for (int64_t r = 32 * s; r < 32 * s + 32 && r < n; ++r) w = std::max(w, rowptr[r + 1] - rowptr[r]);
+    slice_ptr[s + 1] = slice_ptr[s] + 32 * w;
+  }
+  if (!col || !src_pos) return ESR_OK;
+  if (rowptr[n] > 0 && (!perm || !colidx)) return esr::fail(ESR_ERR_ARG, "null perm/colidx");
+  for (int64_t s = 0; s < nslices; ++s) {
+    const int64_t w = (slice_ptr[s + 1] - slice_ptr[s]) / 32;
+    for (int64_t l = 0; l < 32; ++l) {
+      const int64_t r = 32 * s + l;
+      const int64_t len = r < n ? rowptr[r + 1] - rowptr[r] : 0;
+      for (int64_t k = 0; k < w; ++k) {
+        const int64_t pos = slice_ptr[s] + 32 * k + l;
+        if (k < len) {
+          const int64_t e = perm[rowptr[r] + k];
+          const int64_t c = colidx[e];
+          if (c < 0 || c >= ncols)
+            return esr::fail(ESR_ERR_ARG, "selector index " + std::to_string(c) + " out of range [0, " +
+                                              std::to_string(ncols) + ")");
+          col[pos] = (int32_t)c;
+          src_pos[pos] = e;
+        } else {
+          col[pos] = -1;
+          src_pos[pos] = -1;
+        }
+      }
+    }
+  }
+  return ESR_OK;
+}

@@ -1,0 +1,193 @@
+"""SELL-32 matrices built from a ``Linsys`` and the fused PCG driver.
+
+``SellMatrix.from_linsys`` turns ``A(x) = reducer(selector(x)*Ae) + x*Av``
+into the slot-major SELL-32 layout of ``include/esr_gb300.h`` (rows = the
+Reducer index, columns = the Selector index, entries of a row in the
+reference's edge order).  ``FusedPCG`` runs (P)CG on it with the device-side
+stopping test, launching iterations in chunks captured in a CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+import torch
+
+from .. import _lib, mesh
+
+
+class SellMatrix:
+    def __init__(self, n: int, slice_ptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor, diag: torch.Tensor,
+                 src_pos: Optional[torch.Tensor] = None):
+        self.n = n
+        self.slice_ptr = slice_ptr
+        self.col = col
+        self.val = val
+        self.diag = diag
+        self.src_pos = src_pos
+        self.dtype = val.dtype
+        self.device = val.device
+        self.nnz = int((col >= 0).sum().item()) if col.numel() else 0
+        self.desc = _lib.Sell(n, col.numel(), _lib.dtype_code(val.dtype), 0, _lib.ptr(slice_ptr), _lib.ptr(col),
+                              _lib.ptr(val), _lib.ptr(diag))
+
+    @staticmethod
+    def layout(n: int, row_idx: np.ndarray, col_idx: np.ndarray):
+        rowptr, perm = mesh.csr_from_index(row_idx, n)
+        return mesh.sell_layout(n, rowptr, perm, col_idx, n)
+
+    @classmethod
+    def from_arrays(cls, n: int, row_idx: np.ndarray, col_idx: np.ndarray, Ae: torch.Tensor, Av: torch.Tensor,
+                    dtype: Optional[torch.dtype] = None, layout=None) -> "SellMatrix":
+        dev = Av.device
+        dtype = dtype or Av.dtype
+        slice_ptr, col, src_pos = layout if layout is not None else cls.layout(n, row_idx, col_idx)
+        sp = torch.from_numpy(slice_ptr).to(dev)
+        c = torch.from_numpy(col).to(dev)
+        pos = torch.from_numpy(src_pos).to(dev)
+        valid = pos >= 0
+        ae = Ae.to(dev)
+        val = torch.where(valid, ae[torch.where(valid, pos, torch.zeros_like(pos))],
+                          torch.zeros(1, dtype=ae.dtype, device=dev)).to(dtype).contiguous()
+        return cls(n, sp, c, val, Av.to(dtype).contiguous(), pos)
+
+    @classmethod
+    def from_linsys(cls, A, dtype: Optional[torch.dtype] = None) -> "SellMatrix":
+        sel, red = A.selector, A.reducer
+        n = A.Av.shape[0]
+        if red.n != n:
+            raise ValueError(f"Linsys reducer has n={red.n} rows but Av has {n}")
+        row = red.idx.detach().cpu().numpy().astype(np.int64)
+        col = sel.idx.detach().cpu().numpy().astype(np.int64)
+        return cls.from_arrays(n, row, col, A.Ae.data, A.Av.data, dtype)
+
+    def astype(self, dtype: torch.dtype) -> "SellMatrix":
+        return SellMatrix(self.n, self.slice_ptr, self.col, self.val.to(dtype), self.diag.to(dtype), self.src_pos)
+
+    def spmv(self, x: torch.Tensor, y: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """y = A x, bitwise the reference's Linsys.forward."""
+        if y is None:
+            y = torch.empty_like(x)
+        _lib.call("esr_spmv", ctypes.byref(self.desc), _lib.ptr(x), _lib.ptr(y), _lib.stream_handle(self.device))
+        return y
+
+    def bytes_per_spmv(self) -> int:
+        s = self.val.element_size()
+        return self.col.numel() * (4 + s) + self.slice_ptr.numel() * 8 + self.n * (3 * s)
+
+
+class FusedPCG:
+    """Jacobi- or un-preconditioned CG on a SELL matrix (cg.py algorithm)."""
+
+    def __init__(self, A: SellMatrix, jacobi: bool = False, chunk: int = 32, use_graph: bool = True):
+        self.A = A
+        self.n = A.n
+        self.dev = A.device
+        self.dtype = A.dtype
+        self.invdiag = (1.0 / A.diag).contiguous() if jacobi else None
+        self.ws = torch.zeros(int(_lib.lib().esr_cg_workspace_bytes(self.n)), dtype=torch.uint8, device=self.dev)
+        self.q = torch.empty(self.n, dtype=self.dtype, device=self.dev)
+        self.chunk = chunk
+        self.use_graph = use_graph
+        self._graphs = {}
+        self.kernel_launches = 0
+
+    def _iterate_call(self, x, r, z, p, k):
+        _lib.call("esr_cg_iterate", ctypes.byref(self.A.desc), _lib.ptr(x), _lib.ptr(r), _lib.ptr(z), _lib.ptr(p),
+                  _lib.ptr(self.q), _lib.ptr(self.invdiag), int(k), _lib.ptr(self.ws), _lib.stream_handle(self.dev))
+
+    def _chunk(self, x, r, z, p, k):
+        key = (x.data_ptr(), r.data_ptr(), z.data_ptr(), p.data_ptr(), k)
+        if not self.use_graph:
+            self._iterate_call(x, r, z, p, k)
+            return
+        g = self._graphs.get(key)
+        if g is None:
+            # capture on a side stream, as torch requires
+            s = torch.cuda.Stream(self.dev)
+            s.wait_stream(torch.cuda.current_stream(self.dev))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self._iterate_call(x, r, z, p, k)
+            torch.cuda.current_stream(self.dev).wait_stream(s)
+            self._graphs[key] = g
+        g.replay()
+
+    def scalars(self) -> _lib.CgScalars:
+        out = _lib.CgScalars()
+        _lib.call("esr_cg_read_scalars", _lib.ptr(self.ws), ctypes.byref(out), _lib.stream_handle(self.dev))
+        return out
+
+    def solve(self, b, x, r, z, p, rtol: float, atol: Optional[float], maxiter: Optional[int]) -> _lib.CgScalars:
+        """Runs to convergence; x is updated in place.  Returns the final
+        device scalars (iters = number of step() calls)."""
+        _lib.call("esr_cg_init", ctypes.byref(self.A.desc), _lib.ptr(b), _lib.ptr(x), _lib.ptr(r), _lib.ptr(z),
+                  _lib.ptr(p), _lib.ptr(self.invdiag), float(rtol), float(atol) if atol else 0.0,
+                  -1 if maxiter is None else int(maxiter), _lib.ptr(self.ws), _lib.stream_handle(self.dev))
+        self.kernel_launches += 1
+        k = max(1, min(self.chunk, 8))
+        while True:
+            self._chunk(x, r, z, p, k)
+            self.kernel_launches += 3 * k
+            s = self.scalars()
+            if s.done:
+                return s
+            k = min(self.chunk, 2 * k)
+
+    def true_residual(self, b, x, r_scratch) -> float:
+        out = torch.empty(1, dtype=torch.float64, device=self.dev)
+        _lib.call("esr_true_residual", ctypes.byref(self.A.desc), _lib.ptr(b), _lib.ptr(x), _lib.ptr(r_scratch),
+                  _lib.ptr(out), _lib.ptr(self.ws), _lib.stream_handle(self.dev))
+        return float(out.item())
+
+
+class MixedPCG:
+    """FP32-SpMV / FP64-dot CG inside FP64 iterative refinement.
+
+    Outer loop (FP64): r = b - A64 x (exact FP64 SpMV, the true residual);
+    stop when ||r|| <= tol.  Inner: FP32 Jacobi-PCG on A32 d = r/||r|| with
+    FP64-class dot accumulation, to `inner_rtol`; then x += ||r|| * d.
+    """
+
+    def __init__(self, A64: SellMatrix, jacobi: bool = True, inner_rtol: float = 1e-3, chunk: int = 32,
+                 use_graph: bool = True):
+        self.A64 = A64
+        self.A32 = A64.astype(torch.float32)
+        self.inner = FusedPCG(self.A32, jacobi=jacobi, chunk=chunk, use_graph=use_graph)
+        self.outer = FusedPCG(A64, jacobi=False, chunk=chunk, use_graph=False)
+        n, dev = A64.n, A64.device
+        self.r64 = torch.empty(n, dtype=torch.float64, device=dev)
+        self.rhs32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.d32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.r32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.z32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.p32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.inner_rtol = inner_rtol
+        self.inner_iters = 0
+        self.outer_iters = 0
+
+    def solve(self, b, x, rtol: float, atol: Optional[float], maxiter: Optional[int]):
+        dev = self.A64.device
+        stream = _lib.stream_handle(dev)
+        bnorm = float(torch.linalg.vector_norm(b).item())
+        tol = rtol * bnorm
+        if atol and atol > tol:
+            tol = atol
+        self.inner_iters = 0
+        self.outer_iters = 0
+        budget = None if maxiter is None else int(maxiter)
+        while True:
+            rn = self.outer.true_residual(b, x, self.r64)
+            if rn <= tol or (budget is not None and self.inner_iters >= budget) or not np.isfinite(rn):
+                return rn, bnorm
+            self.outer_iters += 1
+            _lib.call("esr_convert", _lib.F64, _lib.ptr(self.r64), _lib.F32, _lib.ptr(self.rhs32), self.A64.n,
+                      1.0 / rn, stream)
+            self.d32.zero_()
+            inner_tol = max(self.inner_rtol, 0.5 * tol / rn)
+            left = None if budget is None else max(budget - self.inner_iters, 0)
+            s = self.inner.solve(self.rhs32, self.d32, self.r32, self.z32, self.p32, inner_tol, None, left)
+            self.inner_iters += s.iters
+            _lib.call("esr_axpy_f64", _lib.ptr(x), _lib.F32, _lib.ptr(self.d32), rn, self.A64.n, stream)

@@ -1,0 +1,326 @@
+/*
+ * esr_gb300.h -- C ABI of the GB300 (sm_103a) sparse-mesh hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (ESR_OK == 0).  On a non-zero status,
+ * esr_last_error() returns a message for the calling host thread.
+ *
+ * Device entry points are stream-ordered on the caller's `stream`
+ * (a cudaStream_t passed as void*; NULL = legacy default stream) and never
+ * synchronise the host.  The library never allocates device memory: any
+ * scratch a kernel needs is passed in by the caller, sized by the matching
+ * *_workspace_bytes() query.
+ *
+ * Index arrays on the device are int32 (the reference stores int64; the host
+ * side narrows them once, after checking every value fits).
+ *
+ * Citations name the reference function each entry point replaces
+ * (paths relative to the EASIER source tree).
+ */
+#ifndef ESR_GB300_H
+#define ESR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ESR_GB300_ABI_VERSION 1
+
+/* element types */
+enum {
+  ESR_F32 = 0,
+  ESR_F64 = 1,
+  ESR_I32 = 2,
+  ESR_I64 = 3
+};
+
+/* Reducer reduce ops: easier/core/module.py:386 (ReduceOp) */
+enum {
+  ESR_REDUCE_SUM = 0,
+  ESR_REDUCE_PROD = 1,
+  ESR_REDUCE_MEAN = 2,
+  ESR_REDUCE_AMAX = 3,
+  ESR_REDUCE_AMIN = 4
+};
+
+/* aggregators: easier/core/module.py:825-884 (sum, prod, norm, max, min) */
+enum {
+  ESR_AGG_SUM = 0,
+  ESR_AGG_PROD = 1,
+  ESR_AGG_NORM = 2,
+  ESR_AGG_MAX = 3,
+  ESR_AGG_MIN = 4
+};
+
+/* status codes */
+enum {
+  ESR_OK = 0,
+  ESR_ERR_ARG = 1,        /* bad argument (size, dtype, null pointer)      */
+  ESR_ERR_CUDA = 2,       /* a CUDA runtime call or launch failed          */
+  ESR_ERR_DEVICE = 3,     /* a kernel reported an error (e.g. idx range)   */
+  ESR_ERR_UNSUPPORTED = 4 /* shape/type combination not implemented        */
+};
+
+/* device-side error bits, OR-ed into the library's device status word */
+enum {
+  ESR_DEV_IDX_RANGE = 1,  /* an index was outside [0, n_in)                */
+  ESR_DEV_NONFINITE = 2   /* a solver produced NaN/Inf                     */
+};
+
+const char *esr_last_error(void);
+int esr_abi_version(void);
+
+/* Read (and optionally clear) the device status word of the current device.
+ * Synchronises `stream` first. */
+int esr_device_status(int *status_out, int clear, void *stream);
+
+/* ------------------------------------------------------------------------ *
+ * Host-side mesh, geometry and ordering (integer work is bit-exact).
+ * ------------------------------------------------------------------------ */
+
+/* Sizes of the unit-square triangular mesh with 4 triangles per square.
+ * Replaces csrc/triangular_mesh.cpp:10-16 (get_mesh size formulas). */
+int esr_mesh_sizes(int64_t n, int64_t *nc, int64_t *ne, int64_t *nbc,
+                   int64_t *np);
+
+/* Unit-square triangular mesh: src/dst [ne], cells [nc*3], bcells [nbc],
+ * bpoints [nbc*2], points [np*2].  Index-for-index identical to
+ * csrc/triangular_mesh.cpp:10-143 (get_mesh). */
+int esr_mesh_triangular(int64_t n, int64_t *src, int64_t *dst, int64_t *cells,
+                        int64_t *bcells, int64_t *bpoints, double *points);
+
+/* Shallow-water geometry: per edge sx, sy, alpha [ne]; per cell area, x, y
+ * [nc]; per boundary face bsx, bsy [nbc].  Same operation order as
+ * tutorial/shallow_water_equation/assemble_shallow_water.py:154-253
+ * (ShallowWaterInitializer.get_alpha/get_face_norm/forward), so the values
+ * are bit-identical to the reference's CPU run. */
+int esr_swe_geometry(int64_t nc, int64_t ne, int64_t nbc, const int64_t *src,
+                     const int64_t *dst, const int64_t *cells,
+                     const int64_t *bcells, const int64_t *bpoints,
+                     const double *points, double *sx, double *sy,
+                     double *alpha, double *area, double *x, double *y,
+                     double *bsx, double *bsy);
+
+/* Cell-centred finite-volume Poisson assembly: Af [ne], Ac, b, rho [nc],
+ * centroid [nc*2].  Follows tutorial/poisson/assemble_poisson.py:160-230
+ * (PoissonInitializer.forward); Ac uses an in-order segment sum like the
+ * reference's Reducer. */
+int esr_poisson_fv_assemble(int64_t nc, int64_t ne, int64_t nbc,
+                            const int64_t *src, const int64_t *dst,
+                            const int64_t *cells, const int64_t *bcells,
+                            const int64_t *bpoints, const double *points,
+                            double *Af, double *Ac, double *b, double *rho,
+                            double *centroid);
+
+/* Sizes of the P1 finite-element Poisson system on an n x n square grid
+ * split into 2 right triangles per square (diagonal (i,j)-(i+1,j+1)), zero
+ * Dirichlet boundary: unknowns = (n-1)^2 interior nodes, nnz_off = number
+ * of directed off-diagonal couplings (6 per interior node minus the ones
+ * that reach the boundary). */
+int esr_p1_sizes(int64_t n, int64_t *nunk, int64_t *nnz_off);
+
+/* P1 stiffness in Linsys form (easier/numeric/linsys.py:10-24): row/col
+ * [nnz_off] (row sorted ascending, the Reducer/Selector idx), Ae [nnz_off]
+ * off-diagonal values, Av [nunk] diagonal.  kappa [2*n*n] is the
+ * per-triangle coefficient (lower triangle of square (i,j) at 2*(j*n+i),
+ * upper at 2*(j*n+i)+1); NULL means kappa = 1.  No reference counterpart
+ * (the reference ships only the FV discretisation). */
+int esr_p1_assemble(int64_t n, const double *kappa, int64_t *row, int64_t *col,
+                    double *Ae, double *Av);
+
+/* Stable counting sort of idx[m] (values in [0, n)): rowptr [n+1] and
+ * perm [m] with perm[k] = original position of the k-th element in
+ * ascending-key, original-order-within-key order.  This is the edge order
+ * the reference's reorder produces at world size 1:
+ * easier/core/passes/sparse_encoding/sparse_encoding.py:244-338
+ * (reorder_input_by_reducer) + easier/core/passes/utils.py:301-336
+ * (zipsort_using_order, stable=True).  Returns ESR_ERR_ARG if any value is
+ * out of range (easier/core/passes/collective_initialization.py:76-106). */
+int esr_csr_from_index(const int64_t *idx, int64_t m, int64_t n,
+                       int64_t *rowptr, int64_t *perm);
+
+/* Reverse Cuthill-McKee ordering of an undirected graph given by directed
+ * edge lists (both directions need not be present; self loops ignored).
+ * order[k] = old vertex placed at new position k.  Deterministic: start of
+ * each component = pseudo-peripheral vertex found from the lowest-degree,
+ * lowest-index unvisited vertex; neighbours visited by (degree, index). */
+int esr_rcm_order(int64_t n, int64_t m, const int64_t *src, const int64_t *dst,
+                  int64_t *order);
+
+/* ------------------------------------------------------------------------ *
+ * Selector / Reducer / aggregators (device).
+ * ------------------------------------------------------------------------ */
+
+/* y[e, :] = x[idx[e], :] for e in [0, m); a row is row_bytes bytes.
+ * Replaces easier/core/module.py:364-371 (Selector.forward).  Indices out
+ * of [0, n_in) set ESR_DEV_IDX_RANGE in the device status word and that row
+ * is left unwritten. */
+int esr_gather(const void *x, int64_t n_in, int64_t row_bytes,
+               const int32_t *idx, int64_t m, void *y, void *stream);
+
+/* Deterministic segmented reduce over a CSR segmentation:
+ *   out[i, c] = op over k in [rowptr[i], rowptr[i+1]) of t[perm ? perm[k] : k, c]
+ * in ascending k (the reference's in-segment edge order).  Rows with an empty
+ * segment keep `out` unchanged (scatter_reduce_ with include_self=False).
+ * Replaces easier/core/module.py:441-461 (Reducer.forward).
+ * dtype: ESR_F32/F64/I32/I64; op: ESR_REDUCE_*. */
+int esr_segreduce(int dtype, int op, const void *t, int64_t row_elems,
+                  const int32_t *rowptr, const int32_t *perm, int64_t n,
+                  void *out, void *stream);
+
+/* Bytes of scratch esr_aggregate needs for an [n, cols] input. */
+int64_t esr_aggregate_workspace_bytes(int64_t n, int64_t cols);
+
+/* out[c] = agg over rows r of t[r, c] (dim 0, keepdim).  Floating inputs
+ * accumulate in FP64 with a fixed two-level tree (deterministic); the
+ * result is stored in the input dtype.  Replaces the local part of
+ * easier/core/module.py:825-884 (esr.sum/prod/norm/max/min); at world size
+ * 1 the allgather that dataflow_distribution.py:197-289 inserts is the
+ * identity, so this is the whole aggregator. */
+int esr_aggregate(int dtype, int agg, const void *t, int64_t n, int64_t cols,
+                  void *out, void *workspace, void *stream);
+
+/* Bytes of scratch esr_dot needs for length-n vectors. */
+int64_t esr_dot_workspace_bytes(int64_t n);
+
+/* out_f64[0] = sum_i a[i]*b[i], FP64 accumulation, fixed tree order.
+ * The CG dot product (easier/numeric/solver/cg.py:70-71, 92). */
+int esr_dot(int dtype, const void *a, const void *b, int64_t n,
+            double *out_f64, void *workspace, void *stream);
+
+/* ------------------------------------------------------------------------ *
+ * Fused shallow-water step (ELL face-slot layout, see esr_swe_mesh).
+ * ------------------------------------------------------------------------ */
+
+/* Face-slot mesh: every cell has `width` face slots stored slot-major
+ * ([slot][cell]).  nbr = neighbour cell (>= 0, an interior edge
+ * src -> this cell), -1 = boundary face, -2 = empty.  Interior slots come
+ * first, in the reference's edge order; then boundary faces.  For an
+ * interior slot sx/sy/alpha are the edge's values; for a boundary slot
+ * sx/sy hold bsx/bsy and alpha is unused. */
+typedef struct {
+  int64_t nc;
+  int32_t width;     /* 3 or 4 */
+  int32_t dtype;     /* ESR_F32 or ESR_F64 (of sx/sy/alpha/area) */
+  const int32_t *nbr;
+  const void *sx;
+  const void *sy;
+  const void *alpha;
+  const void *area;
+} esr_swe_mesh;
+
+/* Scratch bytes for esr_swe_step: two stage states + one accumulator, each
+ * nc x 4 elements. */
+int64_t esr_swe_workspace_bytes(const esr_swe_mesh *mesh);
+
+/* `steps` explicit steps of the reference scheme
+ * (tutorial/shallow_water_equation/swe_main.py:86-141: face_reconstruct,
+ * delta, forward with stage weights 1/6 each) on the cell state
+ * `state` [nc][4] = (h, uh, vh, unused), updated in place.
+ * Every floating operation is issued in the reference's order with
+ * round-to-nearest and no contraction, so FP64/FP32 results are bitwise
+ * those of the reference's CPU backend on the same (reordered) inputs. */
+int esr_swe_step(const esr_swe_mesh *mesh, double dt, void *state,
+                 int64_t steps, void *workspace, void *stream);
+
+/* One `delta` evaluation (swe_main.py:90-119) on state [nc][4]; writes
+ * delta [nc][4] = (delta_h, delta_uh, delta_vh, 0). */
+int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *delta,
+                  void *stream);
+
+/* ------------------------------------------------------------------------ *
+ * Linsys SpMV and fused (P)CG.
+ * ------------------------------------------------------------------------ */
+
+/* SELL-32 form of Linsys (easier/numeric/linsys.py:23-24):
+ *   y[i] = (sum_k x[col[k]] * val[k], k in row i, in order) + x[i] * diag[i].
+ * Rows are grouped in slices of 32; slice s stores its entries slot-major:
+ * entry (slot k, lane l) of slice s lives at slice_ptr[s] + 32*k + l and
+ * belongs to row 32*s + l.  col = -1 marks padding.  Within a row the slots
+ * keep the reference's edge order. */
+typedef struct {
+  int64_t n;                 /* rows (= columns)                        */
+  int64_t nslots;            /* stored entries incl. padding            */
+  int32_t dtype;             /* of val/diag: ESR_F32 or ESR_F64         */
+  int32_t pad_;
+  const int64_t *slice_ptr;  /* [ceil(n/32) + 1]                        */
+  const int32_t *col;        /* [nslots]                                */
+  const void *val;           /* [nslots]                                */
+  const void *diag;          /* [n]                                     */
+} esr_sell;
+
+/* Host: SELL-32 layout of a Linsys.  rowptr/perm = esr_csr_from_index of
+ * the Reducer idx (rows), colidx [m] = the Selector idx (columns, original
+ * edge order).  Always fills slice_ptr; when col and src_pos are non-NULL
+ * also fills col [nslots] and src_pos [nslots] (original edge index of each
+ * slot, -1 for padding) so the caller can gather Ae into val.  Replaces the
+ * layout work of easier/core/passes/sparse_encoding/sparse_encoding.py
+ * :383-434 (rewrite_reducer_instance) at world size 1. */
+int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *perm,
+                   const int64_t *colidx, int64_t ncols, int64_t *slice_ptr,
+                   int32_t *col, int64_t *src_pos);
+
+/* y = A x; dtype of x/y = A's dtype. Bit-identical to the reference's
+ * index-multiply-scatter-add sequence (no contraction). */
+int esr_spmv(const esr_sell *A, const void *x, void *y, void *stream);
+
+/* Scratch bytes for esr_cg_* on an n-row system. */
+int64_t esr_cg_workspace_bytes(int64_t n);
+
+/* Device-side scalars of a fused CG run (FP64), inside the workspace. */
+typedef struct {
+  double rz;       /* r.z of the current iterate                    */
+  double pq;       /* p.Ap                                           */
+  double alpha;
+  double beta;
+  double rr;       /* r.r  (rnorm^2)                                 */
+  double bnorm;
+  double tol;      /* absolute stopping tolerance on ||r||           */
+  double rz_new;
+  int32_t iters;   /* completed step() calls                        */
+  int32_t done;    /* 1 = converged, 2 = maxiter, 3 = breakdown/NaN  */
+  int32_t maxiter; /* < 0: unlimited                                 */
+  int32_t pad_;
+} esr_cg_scalars;
+
+/* PCG set-up (easier/numeric/solver/cg.py:49-53 Init + :136-139):
+ * r = b - A x, z = M r (invdiag == NULL: identity, else z = r * invdiag),
+ * p = z, bnorm = ||b||, tol = max(rtol*bnorm, atol), rz = r.z. */
+int esr_cg_init(const esr_sell *A, const void *b, void *x, void *r, void *z,
+                void *p, const void *invdiag, double rtol, double atol,
+                int32_t maxiter, void *workspace, void *stream);
+
+/* `k` PCG iterations (cg.py:68-95 Step + Update, with the stopping test of
+ * cg.py:150-153 evaluated on the device).  Iterations after convergence are
+ * no-ops, so the host may launch in chunks and poll
+ * esr_cg_read_scalars(). Vectors q and p2 are scratch of length n. */
+int esr_cg_iterate(const esr_sell *A, void *x, void *r, void *z, void *p,
+                   void *q, const void *invdiag, int32_t k, void *workspace,
+                   void *stream);
+
+/* Copy the device scalars to host memory (synchronises `stream`). */
+int esr_cg_read_scalars(const void *workspace, esr_cg_scalars *out,
+                        void *stream);
+
+/* ||b - A x||_2 in FP64 (true residual); out_f64 on the device.
+ * `r` is scratch of length n (receives b - A x). */
+int esr_true_residual(const esr_sell *A, const void *b, const void *x, void *r,
+                      double *out_f64, void *workspace, void *stream);
+
+/* out[i] = (dtype_out)(scale * (double)in[i]); F32/F64 in either direction.
+ * Used by mixed-precision iterative refinement (no reference counterpart). */
+int esr_convert(int dtype_in, const void *in, int dtype_out, void *out,
+                int64_t n, double scale, void *stream);
+
+/* x[i] += scale * (double)d[i] with x FP64 and d F32 or F64: the refinement
+ * correction of mixed-precision CG (no reference counterpart). */
+int esr_axpy_f64(double *x, int dtype_d, const void *d, double scale,
+                 int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ESR_GB300_H */

@@ -1,0 +1,44 @@
+"""Oracle: conjugate gradient (test infrastructure).
+
+Restates easier/numeric/solver/cg.py (Init :49-53, Step :68-76,
+Update :90-95, CG.solve :130-161) on torch CPU tensors, with an optional
+diagonal (Jacobi) preconditioner M(r) = r / Av.
+"""
+import torch
+
+from .sparse import linsys_apply
+
+
+def cg(row, col, Ae, Av, b, x0=None, rtol=1e-5, atol=None, maxiter=None, jacobi=False):
+    Ae, Av, b = (torch.as_tensor(a, dtype=torch.float64) for a in (Ae, Av, b))
+    A = lambda v: linsys_apply(v, row, col, Ae, Av)  # noqa: E731
+    M = (lambda r: r / Av) if jacobi else (lambda r: r)  # noqa: E731
+    x = torch.zeros_like(b) if x0 is None else torch.as_tensor(x0, dtype=torch.float64).clone()
+    r = b - A(x)
+    z = M(r)
+    p = z.clone()
+    bnorm = torch.linalg.vector_norm(b)
+    tol = rtol * bnorm
+    if atol:
+        tol = max(tol, torch.tensor(atol, dtype=torch.float64))
+    iters = 0
+    while True:
+        Ap = A(p)
+        rz = (r * z).sum()
+        alpha = rz / (p * Ap).sum()
+        r = r - alpha * Ap
+        x = x + alpha * p
+        rnorm = torch.linalg.vector_norm(r)
+        if (not torch.isnan(rnorm) and rnorm <= tol) or (maxiter is not None and iters >= maxiter):
+            break
+        iters += 1
+        z1 = M(r)
+        beta = (r * z1).sum() / rz
+        p = z1 + beta * p
+        z = z1
+    return x, iters, float(rnorm)
+
+
+def true_residual(row, col, Ae, Av, b, x):
+    b = torch.as_tensor(b, dtype=torch.float64)
+    return float(torch.linalg.vector_norm(b - linsys_apply(torch.as_tensor(x), row, col, Ae, Av)))

@@ -1,0 +1,133 @@
+"""Fused shallow-water step on the GPU, through esr.compile(backend='cuda'),
+against the reference's own runs (golden fixtures) and the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import easier_gb300 as esr
+from easier_gb300 import workloads
+from oracle import mesh as omesh
+from oracle import swe as oswe
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(n, steps, dt, dtype, h0, fuse=True):
+    eqn = workloads.make_swe(n, dt=dt, dtype=dtype, h=h0)
+    [eqn] = esr.compile([eqn], "cuda", fuse=fuse)
+    for _ in range(steps):
+        eqn()
+    torch.cuda.synchronize()
+    return eqn, [getattr(eqn, k).collect().cpu().numpy() for k in ("h", "uh", "vh")]
+
+
+@pytest.mark.parametrize("tag,dtype", [("f64", torch.float64), ("f32", torch.float32)])
+def test_tutorial_n10_bitwise_vs_reference(golden, tag, dtype):
+    g = golden(f"swe_n10_{tag}_tutorial.npz")
+    eqn, out = _run(10, int(g["steps"]), float(g["dt"]), dtype, g["h0"])
+    assert getattr(eqn, "easier_fused_engine", None) is not None
+    for k, v in zip(("h", "uh", "vh"), out):
+        assert np.array_equal(v, g[k]), k
+
+
+@pytest.mark.parametrize("tag,dtype", [("f64", torch.float64), ("f32", torch.float32)])
+def test_n100_1000_steps_bitwise_vs_reference(golden, tag, dtype):
+    """The reference's CPU-runnable case at full length (40,000 cells,
+    1,000 steps): bitwise equal to the reference's CPU backend."""
+    g = golden(f"swe_n100_{tag}_1000steps.npz")
+    eqn = workloads.make_swe(100, dt=float(g["dt"]), dtype=dtype, h=g["h0"])
+    [eqn] = esr.compile([eqn], "cuda")
+    eng = eqn.easier_fused_engine
+    eng.step(int(g["steps"]))
+    torch.cuda.synchronize()
+    for k in ("h", "uh", "vh"):
+        v = getattr(eqn, k).collect().cpu().numpy()
+        assert np.array_equal(v, g[k]), k
+    if dtype == torch.float32:
+        # FP32 against the FP64 reference run: the stated 1e-5 relative bar
+        g64 = golden("swe_n100_f64_1000steps.npz")
+        h = eqn.h.collect().cpu().double().numpy()
+        assert np.abs(h - g64["h"]).max() <= 1e-5 * np.abs(g64["h"]).max()
+
+
+def test_per_op_path_equals_fused_path():
+    n, steps = 24, 20
+    m = omesh.triangular_mesh(n)
+    geo = omesh.swe_geometry(m)
+    h0 = 1 + 0.1 * np.exp(-((geo["x"] - 0.3) ** 2 + (geo["y"] - 0.6) ** 2) / 0.02)
+    _, fused = _run(n, steps, 1e-3, torch.float64, h0, fuse=True)
+    eqn, perop = _run(n, steps, 1e-3, torch.float64, h0, fuse=False)
+    assert getattr(eqn, "easier_fused_engine", None) is None
+    for a, b in zip(fused, perop):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_larger_mesh_bitwise_vs_oracle(dtype):
+    n, steps, dt = 150, 5, 5e-4
+    m = omesh.triangular_mesh(n)
+    geo = omesh.swe_geometry(m)
+    h0 = 1 + 0.1 * np.exp(-((geo["x"] - 0.5) ** 2 + (geo["y"] - 0.5) ** 2) / 0.01)
+    p = oswe.SweProblem(m["src"], m["dst"], m["bcells"], geo["sx"], geo["sy"], geo["alpha"], geo["bsx"],
+                        geo["bsy"], geo["area"], dt, dtype)
+    ref = p.run(torch.from_numpy(h0).to(dtype), torch.zeros(m["cells"].shape[0], dtype=dtype),
+                torch.zeros(m["cells"].shape[0], dtype=dtype), steps)
+    _, out = _run(n, steps, dt, dtype, h0)
+    for a, b in zip(out, ref):
+        assert np.array_equal(a, b.numpy())
+
+
+def test_collect_order_and_rcm_layout():
+    eqn = workloads.make_swe(12, dt=1e-3)
+    h_orig = eqn.h.easier_data_loader.fully_load("cpu").numpy()
+    [eqn] = esr.compile([eqn], "cuda")
+    eng = eqn.easier_fused_engine
+    assert eng.reorder == "rcm"
+    assert eqn.h.elempart is not None
+    assert np.array_equal(eqn.h.collect().cpu().numpy(), h_orig)
+    assert np.array_equal(eqn.x.collect().cpu().numpy(), eqn.x.easier_data_loader.fully_load("cpu").numpy())
+    # the state views share the engine's packed buffer
+    assert eqn.h.data.data_ptr() == eng.state.data_ptr()
+
+
+def test_deterministic_and_in_place_writes_respected():
+    eqn = workloads.make_swe(30, dt=5e-4)
+    [eqn] = esr.compile([eqn], "cuda")
+    a0 = eqn.h.collect().clone()
+    for _ in range(10):
+        eqn()
+    a = eqn.h.collect()
+    eqn2 = workloads.make_swe(30, dt=5e-4)
+    [eqn2] = esr.compile([eqn2], "cuda")
+    for _ in range(10):
+        eqn2()
+    assert torch.equal(a, eqn2.h.collect())
+    # an in-place write through the esr.Tensor reaches the fused state
+    eqn.h[:] = 1.0
+    eqn()
+    assert not torch.equal(eqn.h.collect(), a0)
+
+
+def test_delta_matches_oracle():
+    n = 16
+    m = omesh.triangular_mesh(n)
+    geo = omesh.swe_geometry(m)
+    rng = np.random.default_rng(0)
+    h = 1 + 0.1 * rng.random(4 * n * n)
+    uh = 0.01 * rng.standard_normal(4 * n * n)
+    vh = 0.01 * rng.standard_normal(4 * n * n)
+    p = oswe.SweProblem(m["src"], m["dst"], m["bcells"], geo["sx"], geo["sy"], geo["alpha"], geo["bsx"],
+                        geo["bsy"], geo["area"], 1e-3)
+    ref = p.delta(*(torch.from_numpy(a) for a in (h, uh, vh)))
+    eqn = workloads.make_swe(n, dt=1e-3, h=h)
+    [eqn] = esr.compile([eqn], "cuda")
+    eng = eqn.easier_fused_engine
+    st = eng.state.clone()
+    order = eng.order
+    st[:, 1] = torch.from_numpy(uh).cuda()[order]
+    st[:, 2] = torch.from_numpy(vh).cuda()[order]
+    d = eng.delta(st)
+    for j in range(3):
+        got = torch.empty(4 * n * n, dtype=torch.float64)
+        got[order.cpu()] = d[:, j].cpu()
+        assert torch.equal(got, ref[j])
