@@ -120,6 +120,42 @@ def _max_over_ranks(world, v: float) -> float:
 
 
 # ------------------------------------------------------------------ SWE --
+def swe_algorithmic_bytes(nc, ne, nbc, s):
+    """Bytes of one time step under the per-delta byte model: per delta
+    ne*(4+3s) [src idx, sx, sy, alpha] + nc*(3s+s+4+3s) [state, area,
+    rowptr, delta] + nbc*(4+2s) [wall idx, bsx, bsy]; per step 4 deltas +
+    nc*3s*6 for the stage combination (state, 4 deltas, state out)."""
+    b_delta = ne * (4 + 3 * s) + nc * (3 * s + s + 4 + 3 * s) + nbc * (4 + 2 * s)
+    return 4 * b_delta + nc * 3 * s * 6
+
+
+def swe_f64_secondary(args, dev, stream):
+    """The same workload in FP64 (the reference's precision), fewer steps."""
+    import easier_gb300 as esr
+    from easier_gb300 import workloads
+    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=torch.float64)
+    [eqn] = esr.compile([eqn], "cuda")
+    eng = eqn.easier_fused_engine
+    eng.step(3)
+    steps = max(10, args.steps // 10)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    eng.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    ok = bool(torch.isfinite(eng.state).all())
+    b = swe_algorithmic_bytes(eng.nc, eng.b["ne"], eng.b["nbc"], 8)
+    res = {"value": eng.nc * steps / (ms / 1e3), "unit": "cell-steps/s", "steps": steps,
+           "ms_per_step": ms / steps, "finite": ok,
+           "hbm_frac_of_measured": b / (ms / steps / 1e3) / 1e9 / _peaks()[0],
+           "bound": "fp64 pipe (GB300 FP64 rate is 1/59 of FP32; see DESIGN.md)"}
+    del eqn, eng
+    torch.cuda.empty_cache()
+    return res
+
+
 def swe_cpu_baseline(n, dtype, dt, steps):
     """Oracle SWE step on the host cores; returns (cell-steps/s, threads)."""
     from easier_gb300 import mesh
@@ -169,9 +205,13 @@ def bench_swe(args, world, rank, local):
     if not bool(torch.isfinite(h).all()):
         raise RuntimeError("non-finite shallow-water state after the timed steps")
     value = world * nc * args.steps / (ms_max / 1e3)
-    bytes_step = eng.workload_bytes_per_step()
+    bytes_step = swe_algorithmic_bytes(nc, eng.b["ne"], eng.b["nbc"], 4 if dtype == torch.float32 else 8)
+    touched = eng.workload_bytes_per_step()
     peak, peak_kind = _peaks()
     achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
+    f64 = None
+    if args.dtype == "f32" and not args.no_f64:
+        f64 = swe_f64_secondary(args, dev, stream)
 
     # end to end through the C ABI with host buffers: every step uploads the
     # packed state from pinned host memory, runs esr_swe_step, reads it back
@@ -215,7 +255,10 @@ def bench_swe(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
                      "kernel": "swe_stage_kernel (4 launches per step; bytes and time per step / 4)",
-                     "algorithmic_bytes_per_launch": bytes_step / 4},
+                     "algorithmic_bytes_per_launch": bytes_step / 4,
+                     "touched_bytes_per_launch": touched / 4,
+                     "touched_frac": touched / (ms / args.steps / 1e3) / 1e9 / peak},
+        "f64": f64,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * args.steps, "clocks": clk.summary(),
     }
     return line
@@ -344,14 +387,20 @@ def main():
     ap.add_argument("--workload", choices=["swe", "poisson"], default="swe")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
-    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--dt", type=float, default=None)
     ap.add_argument("--precision", choices=["native", "mixed"], default="native")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
     args = ap.parse_args()
     if args.n is None:
         args.n = 2000 if args.workload == "swe" else 1000
+    if args.dt is None:
+        # dt = 5e-4 at N=2000 exceeds the scheme's stability limit (the state
+        # turns non-finite within ~200 steps); 2.5e-4 is stable for 1000+
+        # steps.  The per-step cost does not depend on dt.
+        args.dt = 5e-4 if args.n <= 1000 else 2.5e-4
     world, rank, local = _dist()
     if args.impl == "reference":
         if args.steps is None:
