@@ -58,6 +58,7 @@ _SIGS = {
     "esr_segreduce": (c_int, [c_int, c_int, _P, c_int64, _P, _P, c_int64, _P, _P]),
     "esr_aggregate_workspace_bytes": (c_int64, [c_int64, c_int64]),
     "esr_aggregate": (c_int, [c_int, c_int, _P, c_int64, c_int64, _P, _P, _P]),
+    "esr_aggregate_noalloc": (c_int, [c_int, c_int, _P, c_int64, c_int64, _P, _P]),
     "esr_dot_workspace_bytes": (c_int64, [c_int64]),
     "esr_dot": (c_int, [c_int, _P, _P, c_int64, _P, _P, _P]),
     "esr_swe_workspace_bytes": (c_int64, [POINTER(SweMesh)]),

@@ -6,6 +6,7 @@
 // scatter_reduce_ accumulates in, so sums are bitwise equal to it.
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "esr_internal.h"
 #include "reduce_util.cuh"
@@ -394,4 +395,70 @@ extern "C" int esr_dot(int dtype, const void *a, const void *b, int64_t n, doubl
   }
   ESR_LAUNCH_CHECK("esr_dot");
   return ESR_OK;
+}
+
+// ------------------------------------------------------ allocation-free --
+// esr_aggregate_noalloc runs the same two launches as esr_aggregate, but its
+// block partials live in the file-scope device array below instead of a
+// workspace the caller allocates.  It exists for callers that cannot call
+// cudaMalloc at the point where they need an aggregate: cudaMalloc/cudaFree
+// synchronise the whole device (stalling every other stream of a time-step
+// loop or solver), they can fail with out-of-memory in the middle of a run,
+// and some host applications hand all device memory to their own pool and
+// forbid libraries from allocating.  The array is a fixed 1 MiB per device
+// that loaded this library, held until the process exits.
+static __device__ __align__(256) unsigned char g_agg_noalloc_scratch[ESR_AGG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kNoAllocMaxDevices];  // device address of the array, per device
+}  // namespace
+
+extern "C" int esr_aggregate_noalloc(int dtype, int agg, const void *t, int64_t n, int64_t cols, void *out,
+                                     void *stream) {
+  if (n < 0 || cols < 0) return esr::fail(ESR_ERR_ARG, "esr_aggregate_noalloc: negative size");
+  if (cols == 0) return ESR_OK;
+  if (!out || (n && !t)) return esr::fail(ESR_ERR_ARG, "esr_aggregate_noalloc: null pointer");
+  const int64_t need = esr_aggregate_workspace_bytes(n, cols);
+  if (need > (int64_t)ESR_AGG_NOALLOC_SCRATCH_BYTES)
+    return esr::fail(ESR_ERR_ARG, "esr_aggregate_noalloc: n=" + std::to_string(n) + ", cols=" +
+                                      std::to_string(cols) + " needs " + std::to_string(need) +
+                                      " bytes of scratch, more than the " +
+                                      std::to_string((long long)ESR_AGG_NOALLOC_SCRATCH_BYTES) +
+                                      " bytes of the static array (any cols <= " +
+                                      std::to_string(ESR_AGG_NOALLOC_MAX_COLS) +
+                                      " fits); use esr_aggregate with a workspace");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return esr::fail(ESR_ERR_UNSUPPORTED, "esr_aggregate_noalloc: device ordinal");
+  void *ws = nullptr;
+  {
+    // First call on this device: look up the array's device address (this
+    // is the set-up; it may load the module, so it must not be the first
+    // call inside a stream capture).
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_agg_noalloc_scratch);
+      if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/cudaGetSymbolAddress");
+      g_noalloc_addr[dev] = p;
+    }
+    ws = g_noalloc_addr[dev];
+  }
+  // Every partial slot the second launch reads is written by the first one,
+  // so nothing needs clearing between calls.
+  cudaStream_t st = esr::as_stream(stream);
+  switch (dtype) {
+    case ESR_F32: return launch_agg<float>(agg, t, n, cols, out, ws, st);
+    case ESR_F64: return launch_agg<double>(agg, t, n, cols, out, ws, st);
+    case ESR_I32:
+      if (agg == ESR_AGG_NORM) return esr::fail(ESR_ERR_UNSUPPORTED, "norm of an integer tensor");
+      return launch_agg<int32_t>(agg, t, n, cols, out, ws, st);
+    case ESR_I64:
+      if (agg == ESR_AGG_NORM) return esr::fail(ESR_ERR_UNSUPPORTED, "norm of an integer tensor");
+      return launch_agg<int64_t>(agg, t, n, cols, out, ws, st);
+    default: return esr::fail(ESR_ERR_UNSUPPORTED, "esr_aggregate_noalloc: dtype");
+  }
 }

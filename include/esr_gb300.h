@@ -182,6 +182,22 @@ int64_t esr_aggregate_workspace_bytes(int64_t n, int64_t cols);
 int esr_aggregate(int dtype, int agg, const void *t, int64_t n, int64_t cols,
                   void *out, void *workspace, void *stream);
 
+/* Aggregate that allocates nothing and takes no workspace: same result,
+ * bit for bit, as esr_aggregate.  No counterpart in the reference.  Meant
+ * for callers that cannot call cudaMalloc where they aggregate (it
+ * synchronises the device, can fail mid-run, or the host application owns
+ * all device memory).  Its scratch is a static 1 MiB device array per
+ * device, kept until the process exits; sizes needing more
+ * (esr_aggregate_workspace_bytes(n, cols) > ESR_AGG_NOALLOC_SCRATCH_BYTES;
+ * every cols <= ESR_AGG_NOALLOC_MAX_COLS fits) are rejected with
+ * ESR_ERR_ARG.  The first call on a device looks up the array's address
+ * (make that call before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU (different streams, no ordering) race. */
+#define ESR_AGG_NOALLOC_SCRATCH_BYTES (1 << 20)
+#define ESR_AGG_NOALLOC_MAX_COLS 64
+int esr_aggregate_noalloc(int dtype, int agg, const void *t, int64_t n,
+                          int64_t cols, void *out, void *stream);
+
 /* Bytes of scratch esr_dot needs for length-n vectors. */
 int64_t esr_dot_workspace_bytes(int64_t n);
 
