@@ -2,9 +2,12 @@
 
 Workloads (``--workload``):
   swe      shallow water on the tutorial mesh, N=2000 (16,000,000 cells,
-           47,992,000 directed edges), centred Gaussian bump, dt=5e-4; one
-           bench step = one time step (4 fused stage kernels); metric
-           cell-steps/s.  Default dtype f32 (``--dtype f64`` for FP64).
+           47,992,000 directed edges), centred Gaussian bump, dt=2.5e-4 (5e-4
+           is unstable at this resolution); one bench step = one time step
+           (one temporally blocked kernel for FP32); metric cell-steps/s.
+           Default dtype f32, ``--precision fast`` (FMA, reciprocal per face;
+           within 1e-5 of the reference) or ``exact`` (bitwise the reference);
+           the other arithmetic and FP64 are reported under ``secondary``.
   poisson  P1 Poisson, 1000x1000 grid (998,001 unknowns, 5,980,016 directed
            couplings), random-mode RHS, Jacobi-PCG to relative residual 1e-8;
            one bench step = one solve; metric solves/s
@@ -129,31 +132,50 @@ def swe_algorithmic_bytes(nc, ne, nbc, s):
     return 4 * b_delta + nc * 3 * s * 6
 
 
-def swe_f64_secondary(args, dev, stream):
-    """The same workload in FP64 (the reference's precision), fewer steps."""
-    import easier_gb300 as esr
-    from easier_gb300 import workloads
-    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=torch.float64)
-    [eqn] = esr.compile([eqn], "cuda")
-    eng = eqn.easier_fused_engine
-    eng.step(3)
-    steps = max(10, args.steps // 10)
+def _time_steps(eng, steps, dev, stream):
+    eng.step(2)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     eng.step(steps)
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1)
-    ok = bool(torch.isfinite(eng.state).all())
+    return e0.elapsed_time(e1)
+
+
+def swe_secondary(args, eng32, dev, stream):
+    """The other arithmetic of the FP32 engine, and the FP64 step (the
+    reference's precision) in both arithmetics, on fewer steps."""
+    import easier_gb300 as esr
+    from easier_gb300 import workloads
+    out = {}
+    other = "exact" if args.precision == "fast" else "fast"
+    keep = eng32.precision
+    eng32.set_precision(other)
+    steps = max(20, args.steps // 5)
+    ms = _time_steps(eng32, steps, dev, stream)
+    b = swe_algorithmic_bytes(eng32.nc, eng32.b["ne"], eng32.b["nbc"], 4)
+    out[f"f32_{other}"] = {"value": eng32.nc * steps / (ms / 1e3), "unit": "cell-steps/s", "steps": steps,
+                           "ms_per_step": ms / steps, "kernel": "tiled" if eng32.tiled else "staged",
+                           "hbm_frac_of_measured": b / (ms / steps / 1e3) / 1e9 / _peaks()[0]}
+    eng32.set_precision(keep)
+    if args.no_f64:
+        return out
+    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=torch.float64)
+    [eqn] = esr.compile([eqn], "cuda", precision="exact")
+    eng = eqn.easier_fused_engine
     b = swe_algorithmic_bytes(eng.nc, eng.b["ne"], eng.b["nbc"], 8)
-    res = {"value": eng.nc * steps / (ms / 1e3), "unit": "cell-steps/s", "steps": steps,
-           "ms_per_step": ms / steps, "finite": ok,
-           "hbm_frac_of_measured": b / (ms / steps / 1e3) / 1e9 / _peaks()[0],
-           "bound": "fp64 pipe (GB300 FP64 rate is 1/59 of FP32; see DESIGN.md)"}
+    for prec in ("exact", "fast"):
+        eng.set_precision(prec)
+        steps = max(10, args.steps // 50)
+        ms = _time_steps(eng, steps, dev, stream)
+        out[f"f64_{prec}"] = {"value": eng.nc * steps / (ms / 1e3), "unit": "cell-steps/s", "steps": steps,
+                              "ms_per_step": ms / steps, "finite": bool(torch.isfinite(eng.state).all()),
+                              "hbm_frac_of_measured": b / (ms / steps / 1e3) / 1e9 / _peaks()[0],
+                              "bound": "fp64 pipe (GB300 FP64 rate is 1/59 of FP32)"}
     del eqn, eng
     torch.cuda.empty_cache()
-    return res
+    return out
 
 
 def swe_cpu_baseline(n, dtype, dt, steps):
@@ -182,7 +204,7 @@ def bench_swe(args, world, rank, local):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     eqn = workloads.make_swe(args.n, dt=args.dt, dtype=dtype)
-    [eqn] = esr.compile([eqn], "cuda")
+    [eqn] = esr.compile([eqn], "cuda", precision=args.precision)
     eng = eqn.easier_fused_engine
     if eng is None:
         raise RuntimeError("the fused shallow-water engine was not installed")
@@ -206,26 +228,31 @@ def bench_swe(args, world, rank, local):
         raise RuntimeError("non-finite shallow-water state after the timed steps")
     value = world * nc * args.steps / (ms_max / 1e3)
     bytes_step = swe_algorithmic_bytes(nc, eng.b["ne"], eng.b["nbc"], 4 if dtype == torch.float32 else 8)
-    touched = eng.workload_bytes_per_step()
+    touched = eng.touched_bytes_per_step()
+    lps = eng.launches_per_step()
     peak, peak_kind = _peaks()
     achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
-    f64 = None
-    if args.dtype == "f32" and not args.no_f64:
-        f64 = swe_f64_secondary(args, dev, stream)
+    secondary = swe_secondary(args, eng, dev, stream) if args.dtype == "f32" else None
 
     # end to end through the C ABI with host buffers: every step uploads the
-    # packed state from pinned host memory, runs esr_swe_step, reads it back
+    # packed state from pinned host memory, runs one step, reads it back
     host = torch.empty((nc, 4), dtype=dtype, pin_memory=True)
     host.copy_(eng.state)
     ke = max(1, min(args.steps, args.e2e_steps))
+    a = eng.bufs[0]
+    b = eng.bufs[1] if eng.tiled else eng.bufs[0]
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(ke):
-        eng.state.copy_(host, non_blocking=True)
-        _lib.call("esr_swe_step", ctypes.byref(eng._mesh), float(args.dt), _lib.ptr(eng.state), 1,
-                  _lib.ptr(eng.ws), stream.cuda_stream)
-        host.copy_(eng.state, non_blocking=True)
+        a.copy_(host, non_blocking=True)
+        if eng.tiled:
+            _lib.call("esr_swe_tile_step", ctypes.byref(eng._tiles), float(args.dt), _lib.ptr(a), _lib.ptr(b), 1,
+                      stream.cuda_stream)
+        else:
+            _lib.call("esr_swe_step", ctypes.byref(eng._mesh), float(args.dt), _lib.ptr(a), 1,
+                      _lib.ptr(eng.ws), stream.cuda_stream)
+        host.copy_(b, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1)
@@ -234,7 +261,8 @@ def bench_swe(args, world, rank, local):
     e2e = {"value": world * nc * ke / (e2e_ms / 1e3), "unit": "cell-steps/s",
            "h2d_bytes_per_step": host.numel() * host.element_size(),
            "d2h_bytes_per_step": host.numel() * host.element_size(), "steps": ke,
-           "path": "esr_swe_step via ctypes, state [nc,4] from/to pinned host memory each step"}
+           "path": ("esr_swe_tile_step" if eng.tiled else "esr_swe_step") +
+                   " via ctypes, state [nc,4] from/to pinned host memory each step"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -242,7 +270,7 @@ def bench_swe(args, world, rank, local):
         cpu = {"value": v, "unit": "cell-steps/s", "cores": thr, "kind": "port",
                "sample": f"{args.cpu_steps} oracle steps (torch CPU ops, reference op order) at N={args.n}, "
                          f"{args.dtype}, {wall:.1f} s"}
-    traffic = _ncu_traffic("swe", args)
+    traffic = _ncu_traffic("swe_tiled" if eng.tiled else "swe", args)
     line = {
         "metric": "SWE cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -254,12 +282,17 @@ def bench_swe(args, world, rank, local):
                    "l2": "inputs larger than L2 (state+geometry ~%.2f GB)" % (bytes_step / 4 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
-                     "kernel": "swe_stage_kernel (4 launches per step; bytes and time per step / 4)",
-                     "algorithmic_bytes_per_launch": bytes_step / 4,
-                     "touched_bytes_per_launch": touched / 4,
+                     "kernel": ("swe_tile_step_kernel (1 launch per step)" if eng.tiled else
+                                "swe_stage_kernel (4 launches per step; bytes and time per step / 4)"),
+                     "algorithmic_bytes_per_launch": bytes_step / lps,
+                     "touched_bytes_per_launch": touched / lps,
                      "touched_frac": touched / (ms / args.steps / 1e3) / 1e9 / peak},
-        "f64": f64,
-        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * args.steps, "clocks": clk.summary(),
+        "precision": args.precision,
+        "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
+                   "within 1e-5 (FP32) / 1e-10 (FP64) relative of the reference FP64 run after 1,000 steps"),
+        "secondary": secondary,
+        "engine": eng.describe(),
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": lps * args.steps, "clocks": clk.summary(),
     }
     return line
 
@@ -388,7 +421,7 @@ def main():
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
     ap.add_argument("--dt", type=float, default=None)
-    ap.add_argument("--precision", choices=["native", "mixed"], default="native")
+    ap.add_argument("--precision", choices=["native", "mixed", "exact", "fast"], default=None)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -401,6 +434,8 @@ def main():
         # turns non-finite within ~200 steps); 2.5e-4 is stable for 1000+
         # steps.  The per-step cost does not depend on dt.
         args.dt = 5e-4 if args.n <= 1000 else 2.5e-4
+    if args.precision is None:
+        args.precision = "fast" if args.workload == "swe" else "native"
     world, rank, local = _dist()
     if args.impl == "reference":
         if args.steps is None:

@@ -26,7 +26,16 @@ _LIB = None
 class SweMesh(Structure):
     _fields_ = [("nc", c_int64), ("width", c_int32), ("dtype", c_int32),
                 ("nbr", c_void_p), ("sx", c_void_p), ("sy", c_void_p),
-                ("alpha", c_void_p), ("area", c_void_p)]
+                ("alpha", c_void_p), ("area", c_void_p), ("inv_area", c_void_p),
+                ("exact", c_int32), ("pad_", c_int32)]
+
+
+class SweTiles(Structure):
+    _fields_ = [("nc", c_int64), ("ntiles", c_int32), ("dtype", c_int32), ("max_local", c_int32),
+                ("max_l3", c_int32), ("max_own", c_int32), ("pad_", c_int32),
+                ("meta", c_void_p), ("off3", c_void_p), ("offh", c_void_p), ("halo", c_void_p),
+                ("lnbr", c_void_p), ("sx", c_void_p), ("sy", c_void_p), ("alpha", c_void_p), ("area", c_void_p),
+                ("inv_area", c_void_p), ("exact", c_int32), ("pad2_", c_int32)]
 
 
 class Sell(Structure):
@@ -64,6 +73,11 @@ _SIGS = {
     "esr_swe_workspace_bytes": (c_int64, [POINTER(SweMesh)]),
     "esr_swe_step": (c_int, [POINTER(SweMesh), c_double, _P, c_int64, _P, _P]),
     "esr_swe_delta": (c_int, [POINTER(SweMesh), _P, _P, _P]),
+    "esr_swe_tile_smem_bytes": (c_int64, [POINTER(SweTiles)]),
+    "esr_swe_tile_step": (c_int, [POINTER(SweTiles), c_double, _P, _P, c_int64, _P]),
+    "esr_bisect_partition": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P]),
+    "esr_swe_tile_layout": (c_int, [c_int64, _P, _P, c_int64, _P, POINTER(c_int64), POINTER(c_int64), _P, _P, _P,
+                                    _P, _P, _P]),
     "esr_spmv": (c_int, [POINTER(Sell), _P, _P, _P]),
     "esr_cg_workspace_bytes": (c_int64, [c_int64]),
     "esr_cg_init": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_double, c_double, c_int32, _P, _P]),
@@ -74,7 +88,7 @@ _SIGS = {
     "esr_axpy_f64": (c_int, [_P, c_int, _P, c_double, c_int64, _P]),
 }
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 
 def library_path() -> Path:

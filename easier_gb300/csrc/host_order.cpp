@@ -216,3 +216,194 @@ extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *p
   }
   return ESR_OK;
 }
+
+// Recursive BFS bisection: split a vertex set in two by the first half of a
+// BFS order started from a pseudo-peripheral vertex of the set (two sweeps),
+// recurse until every part has at most max_part vertices.  Parts are
+// compact (BFS slabs alternate direction as they shrink) and equal-sized
+// within one vertex.  Deterministic.  part[v] = part number; parts are
+// numbered in depth-first order of the recursion.
+extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, const int64_t *dst,
+                                    int64_t max_part, int64_t *part, int64_t *nparts) {
+  if (n < 0 || m < 0 || max_part < 1) return esr::fail(ESR_ERR_ARG, "bad size");
+  if (!part || !nparts || (m && (!src || !dst))) return esr::fail(ESR_ERR_ARG, "null pointer");
+  for (int64_t e = 0; e < m; ++e)
+    if (src[e] < 0 || src[e] >= n || dst[e] < 0 || dst[e] >= n)
+      return esr::fail(ESR_ERR_ARG, "edge endpoint out of range");
+  std::vector<int64_t> ptr(n + 1, 0);
+  for (int64_t e = 0; e < m; ++e) {
+    if (src[e] == dst[e]) continue;
+    ptr[src[e] + 1]++;
+    ptr[dst[e] + 1]++;
+  }
+  for (int64_t i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
+  std::vector<int64_t> adj(ptr[n]);
+  {
+    std::vector<int64_t> pos(ptr.begin(), ptr.end() - 1);
+    for (int64_t e = 0; e < m; ++e) {
+      if (src[e] == dst[e]) continue;
+      adj[pos[src[e]]++] = dst[e];
+      adj[pos[dst[e]]++] = src[e];
+    }
+  }
+  // label[v] = id of the set v currently belongs to; BFS stays inside it
+  std::vector<int64_t> label(n, 0), mark(n, -1);
+  std::vector<int64_t> verts(n);
+  for (int64_t i = 0; i < n; ++i) verts[i] = i;
+  struct Range {
+    int64_t b, e, id;
+  };
+  std::vector<Range> stack;
+  stack.push_back({0, n, 0});
+  int64_t next_id = 1, out_parts = 0, stamp = 0;
+  std::vector<int64_t> order;
+  order.reserve(n);
+  auto bfs = [&](int64_t b, int64_t e, int64_t id, int64_t start) {
+    // BFS order of verts[b:e] (all with label id) from start; unreached
+    // vertices (other components) are appended in their current order
+    ++stamp;
+    order.clear();
+    order.push_back(start);
+    mark[start] = stamp;
+    size_t h = 0;
+    while (true) {
+      while (h < order.size()) {
+        int64_t v = order[h++];
+        for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+          int64_t w = adj[k];
+          if (label[w] == id && mark[w] != stamp) {
+            mark[w] = stamp;
+            order.push_back(w);
+          }
+        }
+      }
+      if ((int64_t)order.size() == e - b) break;
+      for (int64_t i = b; i < e; ++i)
+        if (mark[verts[i]] != stamp) {
+          mark[verts[i]] = stamp;
+          order.push_back(verts[i]);
+          break;
+        }
+    }
+  };
+  while (!stack.empty()) {
+    Range r = stack.back();
+    stack.pop_back();
+    const int64_t sz = r.e - r.b;
+    if (sz <= max_part) {
+      for (int64_t i = r.b; i < r.e; ++i) part[verts[i]] = out_parts;
+      ++out_parts;
+      continue;
+    }
+    // two sweeps find a vertex at a far end of the set (a pseudo-peripheral
+    // vertex); the BFS from there orders the set along its long axis, so the
+    // halves stay compact (one sweep leaves some long, thin parts)
+    int64_t s = verts[r.b];
+    for (int sweep = 0; sweep < 2; ++sweep) {
+      bfs(r.b, r.e, r.id, s);
+      s = order.back();
+    }
+    bfs(r.b, r.e, r.id, s);
+    std::copy(order.begin(), order.end(), verts.begin() + r.b);
+    const int64_t half = r.b + sz / 2;
+    const int64_t ida = next_id++, idb = next_id++;
+    for (int64_t i = r.b; i < half; ++i) label[verts[i]] = ida;
+    for (int64_t i = half; i < r.e; ++i) label[verts[i]] = idb;
+    stack.push_back({half, r.e, idb});
+    stack.push_back({r.b, half, ida});
+  }
+  *nparts = out_parts;
+  return ESR_OK;
+}
+
+
+// Tiled face-slot layout of the shallow-water step (see esr_swe_tiles).
+// Two calls: with halo == NULL it fills meta and the totals; then with the
+// arrays allocated (halo [total_halo], lnbr/slot_src [3*total_l3],
+// area_src/off3 [..]) it fills them.  Per tile the local list is the tile's
+// cells (ascending), then the rings of in-neighbours at distance 1..4, each
+// ring sorted ascending.  nbr [3][nc] is in tile-major numbering; part[c]
+// must be non-decreasing.
+extern "C" int esr_swe_tile_layout(int64_t nc, const int32_t *nbr, const int64_t *part, int64_t ntiles,
+                                   int32_t *meta, int64_t *total_halo, int64_t *total_l3, int64_t *off3,
+                                   int64_t *offh, int32_t *halo, int32_t *lnbr, int64_t *slot_src,
+                                   int64_t *area_src) {
+  if (nc <= 0 || ntiles <= 0) return esr::fail(ESR_ERR_ARG, "empty layout");
+  if (!nbr || !part || !meta || !total_halo || !total_l3) return esr::fail(ESR_ERR_ARG, "null pointer");
+  const bool fill = halo != nullptr;
+  if (fill && (!off3 || !offh || !lnbr || !slot_src || !area_src)) return esr::fail(ESR_ERR_ARG, "null output");
+  for (int64_t c = 0; c < nc; ++c) {
+    if (part[c] < 0 || part[c] >= ntiles || (c && part[c] < part[c - 1]))
+      return esr::fail(ESR_ERR_ARG, "part must be non-decreasing tile ids");
+    for (int k = 0; k < 3; ++k) {
+      const int32_t g = nbr[k * nc + c];
+      if (g < -2 || g >= nc) return esr::fail(ESR_ERR_ARG, "face slot out of range");
+    }
+  }
+  std::vector<int64_t> mark(nc, -1), lpos(nc, 0);
+  std::vector<int64_t> list, next;
+  int64_t tot_h = 0, tot_3 = 0;
+  int64_t t_begin = 0;
+  for (int64_t t = 0; t < ntiles; ++t) {
+    int64_t t_end = t_begin;
+    while (t_end < nc && part[t_end] == t) ++t_end;
+    const int64_t n0 = t_end - t_begin;
+    list.clear();
+    for (int64_t c = t_begin; c < t_end; ++c) {
+      mark[c] = t;
+      lpos[c] = (int64_t)list.size();
+      list.push_back(c);
+    }
+    int64_t cum[5];
+    cum[0] = n0;
+    size_t fb = 0, fe = list.size();
+    for (int level = 1; level <= 4; ++level) {
+      next.clear();
+      for (size_t q = fb; q < fe; ++q) {
+        const int64_t c = list[q];
+        for (int k = 0; k < 3; ++k) {
+          const int32_t g = nbr[k * nc + c];
+          if (g >= 0 && mark[g] != t) {
+            mark[g] = t;
+            next.push_back(g);
+          }
+        }
+      }
+      std::sort(next.begin(), next.end());
+      fb = list.size();
+      for (int64_t g : next) {
+        lpos[g] = (int64_t)list.size();
+        list.push_back(g);
+      }
+      fe = list.size();
+      cum[level] = (int64_t)list.size();
+    }
+    int32_t *mt = meta + 8 * t;
+    mt[0] = (int32_t)t_begin;
+    for (int q = 0; q < 5; ++q) mt[1 + q] = (int32_t)cum[q];
+    mt[6] = mt[7] = 0;
+    const int64_t n3 = cum[3], nL = cum[4];
+    if (fill) {
+      off3[t] = tot_3;
+      offh[t] = tot_h;
+      for (int64_t j = n0; j < nL; ++j) halo[tot_h + (j - n0)] = (int32_t)list[j];
+      for (int64_t j = 0; j < n3; ++j) {
+        const int64_t c = list[j];
+        for (int k = 0; k < 3; ++k) {
+          const int32_t g = nbr[k * nc + c];
+          const int64_t dst = 3 * tot_3 + k * n3 + j;
+          lnbr[dst] = g >= 0 ? (int32_t)lpos[g] : g;
+          slot_src[dst] = k * nc + c;
+        }
+        area_src[tot_3 + j] = c;
+      }
+    }
+    tot_h += nL - n0;
+    tot_3 += n3;
+    t_begin = t_end;
+  }
+  if (t_begin != nc) return esr::fail(ESR_ERR_ARG, "tile ids skip a value");
+  *total_halo = tot_h;
+  *total_l3 = tot_3;
+  return ESR_OK;
+}

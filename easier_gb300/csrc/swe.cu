@@ -1,29 +1,36 @@
 // Fused shallow-water step: gather of neighbour state, face reconstruction,
 // central flux, per-cell face sum, wall pressure term, division by area and
-// the stage combination, in one kernel per stage (4 per step).
+// the stage combination.
 //
 // Reference: tutorial/shallow_water_equation/swe_main.py
 //   face_reconstruct  :83-85   phi_f = (1 - alpha) * phi[src] + alpha * phi[dst]
 //   delta             :87-119  fluxes, scatter(dst), scatter_b(bcells), / area
 //   forward           :121-141 stage states s + c*delta_k, s += dt/6 * sum_k
 //
-// Layout (all of it stays in HBM between launches):
-//   state  [nc][4]  (h, uh, vh, 0)   16 B (FP32) / 32 B (FP64) per cell
-//   slots  [width][nc] nbr:int32, sx, sy, alpha   slot-major -> coalesced
-//   area   [nc]
+// Two kernels with the same per-cell arithmetic:
+//   * swe_stage_kernel: one launch per stage (4 per step), stage states in
+//     HBM.  Layout: state [nc][4] (h, uh, vh, 0); face slots [width][nc]
+//     (nbr int32, sx, sy, alpha) slot-major; area [nc].
+//   * swe_tile_step_kernel (FP32): one launch per step; a CTA keeps a tile
+//     plus the 4 rings of in-neighbours in shared memory and recomputes the
+//     halo's stage values instead of exchanging them through HBM.
 // One thread owns one cell and walks its face slots in order: interior edges
-// in the reference's edge order, then wall faces.  The per-cell sums are
-// therefore the reference's in-order Reducer sums, and every arithmetic
-// operation is one round-to-nearest IEEE op in the reference's order, so the
-// result is bitwise the reference's CPU result.
+// in the reference's edge order, then wall faces, so the per-cell sums are
+// the reference's in-order Reducer sums.
+//
+// Arithmetic policy (template flag EXACT):
+//   EXACT: every operation is one round-to-nearest IEEE op in the
+//          reference's order (explicit _rn intrinsics: no FMA contraction,
+//          IEEE division) -> bitwise the reference's CPU backend.
+//   fast:  the same formulas with FMA contraction, one reciprocal of h_f per
+//          face for u_f = uh_f/h_f and v_f = vh_f/h_f, and a multiply by a
+//          precomputed 1/area.
 //
 // Stages (c1 = 0.5*dt, c3 = dt, c4 = dt/6, rounded to T like torch does):
 //   1: D1 = delta(s0);           S1 = s0 + c1*D1;  A = D1
 //   2: D2 = delta(S1);           S2 = s0 + c1*D2;  A = A + D2
 //   3: D3 = delta(S2);           S1 = s0 + c3*D3;  A = A + D3
 //   4: D4 = delta(S1);           s0 = s0 + c4*(A + D4)
-// Stage 4 writes s0 in place: it gathers neighbours from S1 and reads s0
-// only at its own cell.
 #include <cstdint>
 
 #include "esr_internal.h"
@@ -33,6 +40,91 @@ namespace {
 
 constexpr int kSweThreads = 256;
 
+template <typename T, bool EXACT>
+struct Ar;
+
+template <typename T>
+struct Ar<T, true> {
+  using O = ops<T>;
+  static __device__ __forceinline__ T mul(T a, T b) { return O::mul(a, b); }
+  static __device__ __forceinline__ T add(T a, T b) { return O::add(a, b); }
+  static __device__ __forceinline__ T sub(T a, T b) { return O::sub(a, b); }
+  // a*b + c, two roundings
+  static __device__ __forceinline__ T madd(T a, T b, T c) { return O::add(O::mul(a, b), c); }
+  static __device__ __forceinline__ T recip(T) { return T(0); }
+  static __device__ __forceinline__ T quot(T x, T y, T) { return O::div(x, y); }
+};
+
+template <>
+struct Ar<float, false> {
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+  static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+  static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+  static __device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ float recip(float y) { return __fdividef(1.0f, y); }
+  static __device__ __forceinline__ float quot(float x, float, float yinv) { return x * yinv; }
+};
+
+template <>
+struct Ar<double, false> {
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static __device__ __forceinline__ double madd(double a, double b, double c) { return fma(a, b, c); }
+  static __device__ __forceinline__ double recip(double y) { return 1.0 / y; }
+  static __device__ __forceinline__ double quot(double x, double, double yinv) { return x * yinv; }
+};
+
+template <typename T>
+struct Acc3 {
+  T Sh, Su, Sv;  // scatter(...) over interior edges
+  T Bu, Bv;      // scatter_b(...) over wall faces
+};
+
+// One interior face of a cell: flux terms of swe_main.py:87-117 added to the
+// cell's sums.  own/nb = (h, uh, vh) of the destination (this cell) and the
+// source (neighbour).
+template <typename T, bool EXACT>
+__device__ __forceinline__ void add_face(Acc3<T> &s, T oh, T ou, T ov, T nh, T nu, T nv, T a, T fx, T fy) {
+  using A = Ar<T, EXACT>;
+  const T half = T(0.5);
+  const T om = A::sub(T(1), a);
+  const T hf = A::madd(om, nh, A::mul(a, oh));   // (1 - alpha)*h[src] + alpha*h[dst]
+  const T uhf = A::madd(om, nu, A::mul(a, ou));
+  const T vhf = A::madd(om, nv, A::mul(a, ov));
+  const T ih = A::recip(hf);
+  const T uf = A::quot(uhf, hf, ih);
+  const T vf = A::quot(vhf, hf, ih);
+  const T hfs = A::mul(A::mul(half, hf), hf);    // 0.5 * h_f * h_f
+  const T uhsx = A::mul(uhf, fx);                // uh_f * sx
+  const T vhsy = A::mul(vhf, fy);                // vh_f * sy
+  const T Fh = A::add(uhsx, vhsy);
+  const T Fu = A::madd(A::madd(uf, uhf, hfs), fx, A::mul(uf, vhsy));
+  const T Fv = A::madd(vf, uhsx, A::mul(A::madd(vf, vhf, hfs), fy));
+  s.Sh = A::add(s.Sh, Fh);
+  s.Su = A::add(s.Su, Fu);
+  s.Sv = A::add(s.Sv, Fv);
+}
+
+// A wall face: 0.5 * gather_b(h)**2 * (bsx, bsy)
+template <typename T, bool EXACT>
+__device__ __forceinline__ void add_wall(Acc3<T> &s, T oh, T fx, T fy) {
+  using A = Ar<T, EXACT>;
+  const T gb = A::mul(T(0.5), A::mul(oh, oh));
+  s.Bu = A::madd(gb, fx, s.Bu);
+  s.Bv = A::madd(gb, fy, s.Bv);
+}
+
+// delta = -(sums) / area
+template <typename T, bool EXACT>
+__device__ __forceinline__ void finish(const Acc3<T> &s, T ar, T iar, T &dh, T &du, T &dv) {
+  using A = Ar<T, EXACT>;
+  dh = A::quot(-s.Sh, ar, iar);
+  du = A::quot(-A::add(s.Su, s.Bu), ar, iar);
+  dv = A::quot(-A::add(s.Sv, s.Bv), ar, iar);
+}
+
+// ----------------------------------------------------------- staged --
 template <typename T>
 struct alignas(4 * sizeof(T)) Vec4 {
   T x, y, z, w;
@@ -58,109 +150,82 @@ __device__ __forceinline__ void store4<double>(double *p, Vec4<double> v) {
   reinterpret_cast<double2 *>(p)[1] = make_double2(v.z, v.w);
 }
 
+template <typename T>
+struct SlotsG {  // face slots in global memory, [width][nc]
+  const int32_t *nbr;
+  const T *sx, *sy, *alpha, *area, *inv_area;
+};
+
 // delta (swe_main.py:87-119) of cell i given the stage state `s`.
-template <typename T, int W>
-__device__ __forceinline__ Vec4<T> cell_delta(int64_t i, int64_t nc, const int32_t *__restrict__ nbr,
-                                              const T *__restrict__ sx, const T *__restrict__ sy,
-                                              const T *__restrict__ alpha, const T *__restrict__ area,
-                                              const T *__restrict__ s, const Vec4<T> own) {
-  using O = ops<T>;
-  const T half = T(0.5);
-  T Sh = T(0), Su = T(0), Sv = T(0);  // scatter(...) over interior edges
-  T Bu = T(0), Bv = T(0);             // scatter_b(...) over wall faces
+template <typename T, int W, bool EXACT>
+__device__ __forceinline__ Vec4<T> cell_delta(int64_t i, int64_t nc, const SlotsG<T> &g, const T *s,
+                                              const Vec4<T> own) {
+  Acc3<T> acc{T(0), T(0), T(0), T(0), T(0)};
 #pragma unroll
   for (int k = 0; k < W; ++k) {
-    const int32_t j = __ldg(nbr + k * nc + i);
+    const int32_t j = __ldg(g.nbr + k * nc + i);
     if (j >= 0) {
       if ((int64_t)j >= nc) {  // corrupt slot: flag it, never read out of bounds
         esr::raise_status(ESR_DEV_IDX_RANGE);
         continue;
       }
-      const T a = __ldg(alpha + k * nc + i);
-      const T fx = __ldg(sx + k * nc + i);
-      const T fy = __ldg(sy + k * nc + i);
       const Vec4<T> nb = load4(s + 4 * (int64_t)j);
-      const T om = O::sub(T(1), a);
-      // face_reconstruct: (1 - alpha) * gather_src + alpha * gather_dst
-      const T hf = O::add(O::mul(om, nb.x), O::mul(a, own.x));
-      const T uhf = O::add(O::mul(om, nb.y), O::mul(a, own.y));
-      const T vhf = O::add(O::mul(om, nb.z), O::mul(a, own.z));
-      const T uf = O::div(uhf, hf);
-      const T vf = O::div(vhf, hf);
-      const T hfs = O::mul(O::mul(half, hf), hf);  // 0.5 * h_f * h_f
-      const T uhsx = O::mul(uhf, fx);               // uh_f * sx
-      const T vhsy = O::mul(vhf, fy);               // vh_f * sy
-      const T Fh = O::add(uhsx, vhsy);
-      const T Fu = O::add(O::mul(O::add(O::mul(uf, uhf), hfs), fx), O::mul(uf, vhsy));
-      const T Fv = O::add(O::mul(vf, uhsx), O::mul(O::add(O::mul(vf, vhf), hfs), fy));
-      Sh = O::add(Sh, Fh);
-      Su = O::add(Su, Fu);
-      Sv = O::add(Sv, Fv);
+      add_face<T, EXACT>(acc, own.x, own.y, own.z, nb.x, nb.y, nb.z, __ldg(g.alpha + k * nc + i),
+                         __ldg(g.sx + k * nc + i), __ldg(g.sy + k * nc + i));
     } else if (j == -1) {
-      // wall face: 0.5 * gather_b(h)**2 * (bsx, bsy)
-      const T fx = __ldg(sx + k * nc + i);
-      const T fy = __ldg(sy + k * nc + i);
-      const T gb = O::mul(half, O::mul(own.x, own.x));
-      Bu = O::add(Bu, O::mul(gb, fx));
-      Bv = O::add(Bv, O::mul(gb, fy));
+      add_wall<T, EXACT>(acc, own.x, __ldg(g.sx + k * nc + i), __ldg(g.sy + k * nc + i));
     }
   }
-  const T ar = __ldg(area + i);
   Vec4<T> d;
-  d.x = O::div(-Sh, ar);
-  d.y = O::div(-O::add(Su, Bu), ar);
-  d.z = O::div(-O::add(Sv, Bv), ar);
+  finish<T, EXACT>(acc, __ldg(g.area + i), EXACT ? T(0) : __ldg(g.inv_area + i), d.x, d.y, d.z);
   d.w = T(0);
   return d;
 }
 
-template <typename T, int W, int STAGE>
+template <typename T, int W, int STAGE, bool EXACT>
 __global__ void __launch_bounds__(kSweThreads)
-swe_stage_kernel(int64_t nc, const int32_t *__restrict__ nbr, const T *__restrict__ sx,
-                 const T *__restrict__ sy, const T *__restrict__ alpha, const T *__restrict__ area,
-                 const T *__restrict__ sin, const T *s0, T *__restrict__ acc, T *sout, T c) {
-  using O = ops<T>;
+swe_stage_kernel(int64_t nc, SlotsG<T> g, const T *__restrict__ sin, const T *s0, T *__restrict__ acc, T *sout,
+                 T c) {
+  using A = Ar<T, EXACT>;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const Vec4<T> own_in = load4(sin + 4 * i);
-  const Vec4<T> d = cell_delta<T, W>(i, nc, nbr, sx, sy, alpha, area, sin, own_in);
+  const Vec4<T> d = cell_delta<T, W, EXACT>(i, nc, g, sin, own_in);
   const Vec4<T> base = (STAGE == 1) ? own_in : load4(s0 + 4 * i);
   Vec4<T> out;
   if (STAGE < 4) {
-    out.x = O::add(base.x, O::mul(c, d.x));
-    out.y = O::add(base.y, O::mul(c, d.y));
-    out.z = O::add(base.z, O::mul(c, d.z));
+    out.x = A::madd(c, d.x, base.x);
+    out.y = A::madd(c, d.y, base.y);
+    out.z = A::madd(c, d.z, base.z);
     out.w = T(0);
     Vec4<T> a;
     if (STAGE == 1) {
       a = d;
     } else {
       const Vec4<T> prev = load4(acc + 4 * i);
-      a.x = O::add(prev.x, d.x);
-      a.y = O::add(prev.y, d.y);
-      a.z = O::add(prev.z, d.z);
+      a.x = A::add(prev.x, d.x);
+      a.y = A::add(prev.y, d.y);
+      a.z = A::add(prev.z, d.z);
       a.w = T(0);
     }
     store4(acc + 4 * i, a);
   } else {
     const Vec4<T> prev = load4(acc + 4 * i);
-    out.x = O::add(base.x, O::mul(c, O::add(prev.x, d.x)));
-    out.y = O::add(base.y, O::mul(c, O::add(prev.y, d.y)));
-    out.z = O::add(base.z, O::mul(c, O::add(prev.z, d.z)));
+    out.x = A::madd(c, A::add(prev.x, d.x), base.x);
+    out.y = A::madd(c, A::add(prev.y, d.y), base.y);
+    out.z = A::madd(c, A::add(prev.z, d.z), base.z);
     out.w = base.w;
   }
   store4(sout + 4 * i, out);
 }
 
-template <typename T, int W>
+template <typename T, int W, bool EXACT>
 __global__ void __launch_bounds__(kSweThreads)
-swe_delta_kernel(int64_t nc, const int32_t *__restrict__ nbr, const T *__restrict__ sx,
-                 const T *__restrict__ sy, const T *__restrict__ alpha, const T *__restrict__ area,
-                 const T *__restrict__ s, T *__restrict__ dout) {
+swe_delta_kernel(int64_t nc, SlotsG<T> g, const T *__restrict__ s, T *__restrict__ dout) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const Vec4<T> own = load4(s + 4 * i);
-  store4(dout + 4 * i, cell_delta<T, W>(i, nc, nbr, sx, sy, alpha, area, s, own));
+  store4(dout + 4 * i, cell_delta<T, W, EXACT>(i, nc, g, s, own));
 }
 
 int check_mesh(const esr_swe_mesh *m) {
@@ -170,40 +235,224 @@ int check_mesh(const esr_swe_mesh *m) {
   if (m->width != 3 && m->width != 4) return esr::fail(ESR_ERR_UNSUPPORTED, "face-slot width must be 3 or 4");
   if (m->dtype != ESR_F32 && m->dtype != ESR_F64) return esr::fail(ESR_ERR_UNSUPPORTED, "mesh dtype");
   if (!m->nbr || !m->sx || !m->sy || !m->alpha || !m->area) return esr::fail(ESR_ERR_ARG, "null mesh array");
+  if (!m->exact && !m->inv_area) return esr::fail(ESR_ERR_ARG, "fast arithmetic needs inv_area");
   return ESR_OK;
 }
 
-template <typename T, int W>
+template <typename T>
+SlotsG<T> slots_of(const esr_swe_mesh *m) {
+  return SlotsG<T>{m->nbr, (const T *)m->sx, (const T *)m->sy, (const T *)m->alpha, (const T *)m->area,
+                   (const T *)m->inv_area};
+}
+
+template <typename T, int W, bool EXACT>
 int run_steps(const esr_swe_mesh *m, double dt, T *state, int64_t steps, T *ws, cudaStream_t st) {
   const int64_t nc = m->nc;
   const int grid = (int)((nc + kSweThreads - 1) / kSweThreads);
   T *S1 = ws;
   T *S2 = ws + 4 * nc;
   T *A = ws + 8 * nc;
-  const int32_t *nbr = m->nbr;
-  const T *sx = (const T *)m->sx, *sy = (const T *)m->sy, *al = (const T *)m->alpha, *ar = (const T *)m->area;
+  const SlotsG<T> g = slots_of<T>(m);
   // scalar constants exactly as the reference forms them in Python (double)
   // and as torch rounds a Python scalar into a tensor op of dtype T
   const T c1 = (T)(0.5 * dt);
   const T c3 = (T)dt;
   const T c4 = (T)(dt / 6);
   for (int64_t s = 0; s < steps; ++s) {
-    swe_stage_kernel<T, W, 1><<<grid, kSweThreads, 0, st>>>(nc, nbr, sx, sy, al, ar, state, state, A, S1, c1);
-    swe_stage_kernel<T, W, 2><<<grid, kSweThreads, 0, st>>>(nc, nbr, sx, sy, al, ar, S1, state, A, S2, c1);
-    swe_stage_kernel<T, W, 3><<<grid, kSweThreads, 0, st>>>(nc, nbr, sx, sy, al, ar, S2, state, A, S1, c3);
-    swe_stage_kernel<T, W, 4><<<grid, kSweThreads, 0, st>>>(nc, nbr, sx, sy, al, ar, S1, state, A, state, c4);
+    swe_stage_kernel<T, W, 1, EXACT><<<grid, kSweThreads, 0, st>>>(nc, g, state, state, A, S1, c1);
+    swe_stage_kernel<T, W, 2, EXACT><<<grid, kSweThreads, 0, st>>>(nc, g, S1, state, A, S2, c1);
+    swe_stage_kernel<T, W, 3, EXACT><<<grid, kSweThreads, 0, st>>>(nc, g, S2, state, A, S1, c3);
+    swe_stage_kernel<T, W, 4, EXACT><<<grid, kSweThreads, 0, st>>>(nc, g, S1, state, A, state, c4);
   }
   ESR_LAUNCH_CHECK("esr_swe_step");
   return ESR_OK;
 }
 
-template <typename T, int W>
+template <typename T, int W, bool EXACT>
 int run_delta(const esr_swe_mesh *m, const T *s, T *d, cudaStream_t st) {
   const int64_t nc = m->nc;
   const int grid = (int)((nc + kSweThreads - 1) / kSweThreads);
-  swe_delta_kernel<T, W><<<grid, kSweThreads, 0, st>>>(nc, m->nbr, (const T *)m->sx, (const T *)m->sy,
-                                                       (const T *)m->alpha, (const T *)m->area, s, d);
+  swe_delta_kernel<T, W, EXACT><<<grid, kSweThreads, 0, st>>>(nc, slots_of<T>(m), s, d);
   ESR_LAUNCH_CHECK("esr_swe_delta");
+  return ESR_OK;
+}
+
+template <typename T, bool EXACT>
+int dispatch_steps(const esr_swe_mesh *m, double dt, void *state, int64_t steps, void *ws, cudaStream_t s) {
+  if (m->width == 3) return run_steps<T, 3, EXACT>(m, dt, (T *)state, steps, (T *)ws, s);
+  return run_steps<T, 4, EXACT>(m, dt, (T *)state, steps, (T *)ws, s);
+}
+
+template <typename T, bool EXACT>
+int dispatch_delta(const esr_swe_mesh *m, const void *state, void *delta, cudaStream_t s) {
+  if (m->width == 3) return run_delta<T, 3, EXACT>(m, (const T *)state, (T *)delta, s);
+  return run_delta<T, 4, EXACT>(m, (const T *)state, (T *)delta, s);
+}
+
+// ------------------------------------------------ temporally blocked step --
+// One launch per step.  Cells are grouped in compact tiles; a CTA loads its
+// tile plus the 4 rings of in-neighbours around it into shared memory and
+// runs all 4 stages there:
+//   stage 1 on cells of level <= 3 (reads s0 of levels <= 4)
+//   stage 2 on levels <= 2, stage 3 on levels <= 1, stage 4 on the tile.
+// Every cell value is computed with the operations of swe_stage_kernel, so
+// the result is bitwise the same for the same EXACT setting.  HBM traffic
+// per step is the tile's geometry (plus the halo's), s0 of tile + halo, and
+// the new state; the stage states never leave the SM.
+constexpr int kTileThreads = 1024;
+constexpr int kTileIters = 6;     // cells of level <= 3 per thread: <= 6 * 1024
+constexpr int kTileOwnIters = 4;  // tile cells per thread: <= 4 * 1024
+
+struct SlotsT {  // one tile's face slots, [3][n3]
+  const int32_t *nb;
+  const float *sx, *sy, *al, *area, *inv_area;
+  int n3, nL;
+};
+
+template <bool EXACT>
+__device__ __forceinline__ void tile_delta(int j, const SlotsT &g, const float *hs, const float *us, const float *vs,
+                                           float &dh, float &du, float &dv) {
+  const float oh = hs[j], ou = us[j], ov = vs[j];
+  Acc3<float> acc{0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int32_t q = __ldg(g.nb + k * g.n3 + j);
+    if (q >= 0) {
+      if (q >= g.nL) {  // corrupt layout: flag, never read outside the tile's list
+        esr::raise_status(ESR_DEV_IDX_RANGE);
+        continue;
+      }
+      add_face<float, EXACT>(acc, oh, ou, ov, hs[q], us[q], vs[q], __ldg(g.al + k * g.n3 + j),
+                             __ldg(g.sx + k * g.n3 + j), __ldg(g.sy + k * g.n3 + j));
+    } else if (q == -1) {
+      add_wall<float, EXACT>(acc, oh, __ldg(g.sx + k * g.n3 + j), __ldg(g.sy + k * g.n3 + j));
+    }
+  }
+  finish<float, EXACT>(acc, __ldg(g.area + j), EXACT ? 0.f : __ldg(g.inv_area + j), dh, du, dv);
+}
+
+template <int STAGE, bool EXACT>
+__device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, const float *hs, const float *us,
+                                           const float *vs, const float *h0, const float *u0, const float *v0,
+                                           float *ho, float *uo, float *vo, float (&acc)[kTileOwnIters][3],
+                                           float c, float4 *sout, int64_t cell_off) {
+  using A = Ar<float, EXACT>;
+#pragma unroll
+  for (int r = 0; r < kTileIters; ++r) {
+    const int j = threadIdx.x + r * kTileThreads;
+    if (j < count) {
+      float dh, du, dv;
+      tile_delta<EXACT>(j, g, hs, us, vs, dh, du, dv);
+      if (STAGE < 4) {
+        ho[j] = A::madd(c, dh, h0[j]);
+        uo[j] = A::madd(c, du, u0[j]);
+        vo[j] = A::madd(c, dv, v0[j]);
+        if (r < kTileOwnIters && j < n0) {
+          if (STAGE == 1) {
+            acc[r][0] = dh;
+            acc[r][1] = du;
+            acc[r][2] = dv;
+          } else {
+            acc[r][0] = A::add(acc[r][0], dh);
+            acc[r][1] = A::add(acc[r][1], du);
+            acc[r][2] = A::add(acc[r][2], dv);
+          }
+        }
+      } else if (r < kTileOwnIters) {
+        float4 o;
+        o.x = A::madd(c, A::add(acc[r][0], dh), h0[j]);
+        o.y = A::madd(c, A::add(acc[r][1], du), u0[j]);
+        o.z = A::madd(c, A::add(acc[r][2], dv), v0[j]);
+        o.w = 0.f;
+        sout[cell_off + j] = o;
+      }
+    }
+  }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(kTileThreads, 1)
+swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
+                     const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
+                     const int32_t *__restrict__ lnbr, const float *__restrict__ gsx, const float *__restrict__ gsy,
+                     const float *__restrict__ gal, const float *__restrict__ garea,
+                     const float *__restrict__ ginv_area, const float4 *__restrict__ sin,
+                     float4 *__restrict__ sout, int64_t nc, int max_local, int max_l3, float c1, float c3,
+                     float c4) {
+  extern __shared__ float smem[];
+  const int t = blockIdx.x;
+  const int32_t *mt = meta + 8 * (int64_t)t;
+  const int cell_off = mt[0], n0 = mt[1], n1 = mt[2], n2 = mt[3], n3 = mt[4], nL = mt[5];
+  float *h0 = smem, *u0 = h0 + max_local, *v0 = u0 + max_local;
+  float *hA = v0 + max_local, *uA = hA + max_l3, *vA = uA + max_l3;
+  float *hB = vA + max_l3, *uB = hB + max_l3, *vB = uB + max_l3;
+  const int64_t hb = offh[t];
+  for (int j = threadIdx.x; j < nL; j += kTileThreads) {
+    const int64_t gcell = j < n0 ? (int64_t)cell_off + j : (int64_t)__ldg(halo + hb + (j - n0));
+    if (gcell < 0 || gcell >= nc) {  // corrupt layout: flag, never read out of bounds
+      esr::raise_status(ESR_DEV_IDX_RANGE);
+      h0[j] = 1.f;
+      u0[j] = 0.f;
+      v0[j] = 0.f;
+      continue;
+    }
+    const float4 s = sin[gcell];
+    h0[j] = s.x;
+    u0[j] = s.y;
+    v0[j] = s.z;
+  }
+  __syncthreads();
+  const int64_t o3 = off3[t];
+  const SlotsT g{lnbr + 3 * o3, gsx + 3 * o3, gsy + 3 * o3, gal + 3 * o3, garea + o3,
+                 EXACT ? nullptr : ginv_area + o3, n3, nL};
+  float acc[kTileOwnIters][3];
+#pragma unroll
+  for (int r = 0; r < kTileOwnIters; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.f;
+  tile_stage<1, EXACT>(n3, n0, g, h0, u0, v0, h0, u0, v0, hA, uA, vA, acc, c1, sout, cell_off);
+  __syncthreads();
+  tile_stage<2, EXACT>(n2, n0, g, hA, uA, vA, h0, u0, v0, hB, uB, vB, acc, c1, sout, cell_off);
+  __syncthreads();
+  tile_stage<3, EXACT>(n1, n0, g, hB, uB, vB, h0, u0, v0, hA, uA, vA, acc, c3, sout, cell_off);
+  __syncthreads();
+  tile_stage<4, EXACT>(n0, n0, g, hA, uA, vA, h0, u0, v0, nullptr, nullptr, nullptr, acc, c4, sout, cell_off);
+}
+
+int64_t tile_smem_bytes(const esr_swe_tiles *T) {
+  return (int64_t)(3 * (int64_t)T->max_local + 6 * (int64_t)T->max_l3) * (int64_t)sizeof(float);
+}
+
+int check_tiles(const esr_swe_tiles *T) {
+  if (!T) return esr::fail(ESR_ERR_ARG, "null tile layout");
+  if (T->dtype != ESR_F32) return esr::fail(ESR_ERR_UNSUPPORTED, "tiled step is FP32 only");
+  if (T->nc <= 0 || T->ntiles <= 0) return esr::fail(ESR_ERR_ARG, "empty tile layout");
+  if (T->max_own > kTileOwnIters * kTileThreads)
+    return esr::fail(ESR_ERR_UNSUPPORTED, "a tile has more than 4096 cells");
+  if (T->max_l3 > kTileIters * kTileThreads)
+    return esr::fail(ESR_ERR_UNSUPPORTED, "a tile plus 3 halo rings has more than 6144 cells");
+  if (T->max_local < T->max_l3 || T->max_l3 < T->max_own) return esr::fail(ESR_ERR_ARG, "inconsistent tile maxima");
+  if (tile_smem_bytes(T) > 227 * 1024) return esr::fail(ESR_ERR_UNSUPPORTED, "tile needs more than 227 KB shared memory");
+  if (!T->meta || !T->off3 || !T->offh || !T->lnbr || !T->sx || !T->sy || !T->alpha || !T->area)
+    return esr::fail(ESR_ERR_ARG, "null tile array");
+  if (!T->exact && !T->inv_area) return esr::fail(ESR_ERR_ARG, "fast arithmetic needs inv_area");
+  return ESR_OK;
+}
+
+template <bool EXACT>
+int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps, cudaStream_t s) {
+  const int64_t smem = tile_smem_bytes(tiles);
+  cudaError_t e = cudaFuncSetAttribute(swe_tile_step_kernel<EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/smem attribute");
+  const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
+  float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
+  for (int64_t k = 0; k < steps; ++k) {
+    swe_tile_step_kernel<EXACT><<<tiles->ntiles, kTileThreads, smem, s>>>(
+        tiles->meta, tiles->off3, tiles->offh, tiles->halo, tiles->lnbr, (const float *)tiles->sx,
+        (const float *)tiles->sy, (const float *)tiles->alpha, (const float *)tiles->area,
+        (const float *)tiles->inv_area, buf[k & 1], buf[(k + 1) & 1], tiles->nc, tiles->max_local, tiles->max_l3,
+        c1, c3, c4);
+  }
+  ESR_LAUNCH_CHECK("esr_swe_tile_step");
   return ESR_OK;
 }
 
@@ -226,12 +475,11 @@ extern "C" int esr_swe_step(const esr_swe_mesh *mesh, double dt, void *state, in
   if (!state || !workspace) return esr::fail(ESR_ERR_ARG, "null state/workspace");
   if (((uintptr_t)state | (uintptr_t)workspace) % 32) return esr::fail(ESR_ERR_ARG, "state/workspace must be 32-byte aligned");
   cudaStream_t s = esr::as_stream(stream);
-  if (mesh->dtype == ESR_F64) {
-    if (mesh->width == 3) return run_steps<double, 3>(mesh, dt, (double *)state, steps, (double *)workspace, s);
-    return run_steps<double, 4>(mesh, dt, (double *)state, steps, (double *)workspace, s);
-  }
-  if (mesh->width == 3) return run_steps<float, 3>(mesh, dt, (float *)state, steps, (float *)workspace, s);
-  return run_steps<float, 4>(mesh, dt, (float *)state, steps, (float *)workspace, s);
+  if (mesh->dtype == ESR_F64)
+    return mesh->exact ? dispatch_steps<double, true>(mesh, dt, state, steps, workspace, s)
+                       : dispatch_steps<double, false>(mesh, dt, state, steps, workspace, s);
+  return mesh->exact ? dispatch_steps<float, true>(mesh, dt, state, steps, workspace, s)
+                     : dispatch_steps<float, false>(mesh, dt, state, steps, workspace, s);
 }
 
 extern "C" int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *delta, void *stream) {
@@ -240,10 +488,27 @@ extern "C" int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *
   if (!state || !delta) return esr::fail(ESR_ERR_ARG, "null state/delta");
   if (((uintptr_t)state | (uintptr_t)delta) % 32) return esr::fail(ESR_ERR_ARG, "state/delta must be 32-byte aligned");
   cudaStream_t s = esr::as_stream(stream);
-  if (mesh->dtype == ESR_F64) {
-    if (mesh->width == 3) return run_delta<double, 3>(mesh, (const double *)state, (double *)delta, s);
-    return run_delta<double, 4>(mesh, (const double *)state, (double *)delta, s);
-  }
-  if (mesh->width == 3) return run_delta<float, 3>(mesh, (const float *)state, (float *)delta, s);
-  return run_delta<float, 4>(mesh, (const float *)state, (float *)delta, s);
+  if (mesh->dtype == ESR_F64)
+    return mesh->exact ? dispatch_delta<double, true>(mesh, state, delta, s)
+                       : dispatch_delta<double, false>(mesh, state, delta, s);
+  return mesh->exact ? dispatch_delta<float, true>(mesh, state, delta, s)
+                     : dispatch_delta<float, false>(mesh, state, delta, s);
+}
+
+extern "C" int64_t esr_swe_tile_smem_bytes(const esr_swe_tiles *tiles) {
+  if (check_tiles(tiles)) return -1;
+  return tile_smem_bytes(tiles);
+}
+
+extern "C" int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
+                                 void *stream) {
+  int st = check_tiles(tiles);
+  if (st) return st;
+  if (steps < 0) return esr::fail(ESR_ERR_ARG, "negative step count");
+  if (steps == 0) return ESR_OK;
+  if (!state_a || !state_b || state_a == state_b) return esr::fail(ESR_ERR_ARG, "need two distinct state buffers");
+  if (((uintptr_t)state_a | (uintptr_t)state_b) % 16) return esr::fail(ESR_ERR_ARG, "state buffers must be 16-byte aligned");
+  cudaStream_t s = esr::as_stream(stream);
+  return tiles->exact ? run_tiles<true>(tiles, dt, state_a, state_b, steps, s)
+                      : run_tiles<false>(tiles, dt, state_a, state_b, steps, s);
 }

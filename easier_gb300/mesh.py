@@ -230,3 +230,13 @@ def sell_layout(n: int, rowptr: np.ndarray, perm: np.ndarray, colidx: np.ndarray
     _lib.call("esr_sell_build", n, _lib.ptr(rowptr), _lib.ptr(perm), _lib.ptr(colidx), ncols,
               _lib.ptr(slice_ptr), _lib.ptr(col), _lib.ptr(src_pos))
     return slice_ptr, col, src_pos
+
+
+def bisect_partition(n: int, src: np.ndarray, dst: np.ndarray, max_part: int):
+    """Recursive-BFS-bisection parts of at most max_part vertices."""
+    src, dst = _i64(src), _i64(dst)
+    part = np.empty(n, np.int64)
+    nparts = ctypes.c_int64()
+    _lib.call("esr_bisect_partition", n, src.shape[0], _lib.ptr(src), _lib.ptr(dst), int(max_part), _lib.ptr(part),
+              ctypes.byref(nparts))
+    return part, int(nparts.value)

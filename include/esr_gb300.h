@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 1
+#define ESR_GB300_ABI_VERSION 2
 
 /* element types */
 enum {
@@ -225,6 +225,9 @@ typedef struct {
   const void *sy;
   const void *alpha;
   const void *area;
+  const void *inv_area; /* 1/area, used when exact == 0 (may be NULL otherwise) */
+  int32_t exact;     /* 1: bitwise the reference; 0: fast arithmetic (see esr_swe_step) */
+  int32_t pad_;
 } esr_swe_mesh;
 
 /* Scratch bytes for esr_swe_step: two stage states + one accumulator, each
@@ -235,9 +238,13 @@ int64_t esr_swe_workspace_bytes(const esr_swe_mesh *mesh);
  * (tutorial/shallow_water_equation/swe_main.py:86-141: face_reconstruct,
  * delta, forward with stage weights 1/6 each) on the cell state
  * `state` [nc][4] = (h, uh, vh, unused), updated in place.
- * Every floating operation is issued in the reference's order with
- * round-to-nearest and no contraction, so FP64/FP32 results are bitwise
- * those of the reference's CPU backend on the same (reordered) inputs. */
+ * With mesh->exact, every floating operation is issued in the reference's
+ * order with round-to-nearest and no contraction, so FP64/FP32 results are
+ * bitwise those of the reference's CPU backend on the same (reordered)
+ * inputs.  With exact == 0 the same formulas run with FMA contraction, one
+ * reciprocal per face for u = uh/h, v = vh/h and a multiply by inv_area
+ * (fewer instructions; FP32 within 1e-5, FP64 within 1e-10 relative of the
+ * reference after 1,000 steps). */
 int esr_swe_step(const esr_swe_mesh *mesh, double dt, void *state,
                  int64_t steps, void *workspace, void *stream);
 
@@ -245,6 +252,70 @@ int esr_swe_step(const esr_swe_mesh *mesh, double dt, void *state,
  * delta [nc][4] = (delta_h, delta_uh, delta_vh, 0). */
 int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *delta,
                   void *stream);
+
+/* Temporally blocked layout of the same step (FP32, 3 face slots per
+ * cell).  Cells are numbered tile-major: tile t owns cells
+ * [cell_off, cell_off + n0).  Its local list is the tile followed by the
+ * rings of in-neighbours at distance 1..4 (the cells a 4-stage step of the
+ * tile depends on), sorted by ring: local j < n1 are levels <= 1, j < n2
+ * levels <= 2, j < n3 levels <= 3, j < nL all.  Per tile:
+ *   meta[8t..8t+5] = cell_off, n0, n1, n2, n3, nL
+ *   halo[offh[t] + j - n0] = global cell of local j >= n0
+ *   per local cell j < n3 and slot k: lnbr/sx/sy/alpha[3*off3[t] + k*n3 + j]
+ *   (lnbr = local index of the neighbour, -1 wall, -2 empty), area[off3[t] + j].
+ * Limits: n0 <= 4096, n3 <= 6144, 12*nL + 24*n3 bytes <= 227 KB. */
+typedef struct {
+  int64_t nc;
+  int32_t ntiles;
+  int32_t dtype;     /* ESR_F32 */
+  int32_t max_local; /* max nL */
+  int32_t max_l3;    /* max n3 */
+  int32_t max_own;   /* max n0 */
+  int32_t pad_;
+  const int32_t *meta;
+  const int64_t *off3;
+  const int64_t *offh;
+  const int32_t *halo;
+  const int32_t *lnbr;
+  const void *sx;
+  const void *sy;
+  const void *alpha;
+  const void *area;
+  const void *inv_area; /* [sum(n3)], used when exact == 0 */
+  int32_t exact;        /* as in esr_swe_mesh */
+  int32_t pad2_;
+} esr_swe_tiles;
+
+/* Shared memory one CTA of esr_swe_tile_step uses, or -1 if the layout is
+ * outside the limits. */
+int64_t esr_swe_tile_smem_bytes(const esr_swe_tiles *tiles);
+
+/* `steps` steps of swe_main.py:121-141, one launch per step, bitwise equal
+ * to esr_swe_step with the same `exact` setting.  Step k reads buffer k%2 and writes the other
+ * ([nc][4] FP32 each, tile-major numbering): the result is in state_a when
+ * `steps` is even, in state_b when odd. */
+int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
+                      void *state_b, int64_t steps, void *stream);
+
+/* Host: partition an undirected graph (directed edge lists) into parts of at
+ * most max_part vertices by recursive BFS bisection (compact, equal-sized
+ * parts); part[v] in [0, *nparts).  No reference counterpart. */
+int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src,
+                         const int64_t *dst, int64_t max_part, int64_t *part,
+                         int64_t *nparts);
+
+/* Host: the arrays of esr_swe_tiles from face slots nbr [3][nc] in a
+ * tile-major numbering and the non-decreasing tile id of every cell.  Call
+ * once with halo == NULL (fills meta [ntiles*8], *total_halo, *total_l3),
+ * then with off3/offh [ntiles], halo [total_halo], lnbr/slot_src
+ * [3*total_l3] and area_src [total_l3] allocated.  slot_src/area_src give
+ * the source index of each tile slot in the [3][nc] face-slot arrays and in
+ * the per-cell area array.  No reference counterpart. */
+int esr_swe_tile_layout(int64_t nc, const int32_t *nbr, const int64_t *part,
+                        int64_t ntiles, int32_t *meta, int64_t *total_halo,
+                        int64_t *total_l3, int64_t *off3, int64_t *offh,
+                        int32_t *halo, int32_t *lnbr, int64_t *slot_src,
+                        int64_t *area_src);
 
 /* ------------------------------------------------------------------------ *
  * Linsys SpMV and fused (P)CG.

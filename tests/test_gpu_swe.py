@@ -131,3 +131,40 @@ def test_delta_matches_oracle():
         got = torch.empty(4 * n * n, dtype=torch.float64)
         got[order.cpu()] = d[:, j].cpu()
         assert torch.equal(got, ref[j])
+
+
+@pytest.mark.parametrize("n", [37, 150])
+def test_tiled_equals_staged_fp32(n, monkeypatch):
+    from easier_gb300 import swe
+    outs = []
+    for mode in ("tiled", "staged"):
+        monkeypatch.setattr(swe, "DEFAULT_MODE", mode)
+        eqn = workloads.make_swe(n, dt=5e-4, dtype=torch.float32)
+        [eqn] = esr.compile([eqn], "cuda")
+        eng = eqn.easier_fused_engine
+        assert eng.tiled == (mode == "tiled")
+        eng.step(7)
+        eqn()
+        outs.append([getattr(eqn, k).collect().cpu() for k in ("h", "uh", "vh")])
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("tag,dtype,tol", [("f32", torch.float32, 1e-5), ("f64", torch.float64, 1e-10)])
+@pytest.mark.parametrize("mode", ["tiled", "staged"])
+def test_fast_precision_within_stated_tolerance(golden, tag, dtype, tol, mode, monkeypatch):
+    """precision='fast' after 1,000 steps at N=100 against the reference's
+    FP64 run: relative max-norm error within 1e-5 (FP32) / 1e-10 (FP64)."""
+    from easier_gb300 import swe
+    monkeypatch.setattr(swe, "DEFAULT_MODE", mode)
+    g = golden(f"swe_n100_{tag}_1000steps.npz")
+    g64 = golden("swe_n100_f64_1000steps.npz")
+    eqn = workloads.make_swe(100, dt=float(g["dt"]), dtype=dtype, h=g["h0"])
+    [eqn] = esr.compile([eqn], "cuda", precision="fast")
+    eng = eqn.easier_fused_engine
+    assert eng.precision == "fast" and eng.tiled == (mode == "tiled" and dtype == torch.float32)
+    eng.step(int(g["steps"]))
+    got = np.concatenate([getattr(eqn, k).collect().cpu().double().numpy() for k in ("h", "uh", "vh")])
+    ref = np.concatenate([g64[k] for k in ("h", "uh", "vh")])
+    # relative max-norm error of the state vector (h, uh, vh)
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
