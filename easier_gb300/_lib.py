@@ -46,7 +46,8 @@ class Sell(Structure):
 class CgScalars(Structure):
     _fields_ = [("rz", c_double), ("pq", c_double), ("alpha", c_double), ("beta", c_double),
                 ("rr", c_double), ("bnorm", c_double), ("tol", c_double), ("rz_new", c_double),
-                ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("pad_", c_int32)]
+                ("rz_prev", c_double), ("true_rr", c_double),
+                ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("replacements", c_int32)]
 
 
 _P = c_void_p
@@ -83,6 +84,10 @@ _SIGS = {
     "esr_cg_init": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_double, c_double, c_int32, _P, _P]),
     "esr_cg_iterate": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_int32, _P, _P]),
     "esr_cg_read_scalars": (c_int, [_P, POINTER(CgScalars), _P]),
+    "esr_cg_mixed_init": (c_int, [POINTER(Sell), POINTER(Sell), _P, _P, _P, _P, _P, _P, _P, c_double, c_double,
+                                  c_int32, _P, _P]),
+    "esr_cg_mixed_iterate": (c_int, [POINTER(Sell), POINTER(Sell), _P, _P, _P, _P, _P, _P, _P, _P, c_int32, _P,
+                                     _P]),
     "esr_true_residual": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P]),
     "esr_convert": (c_int, [c_int, _P, c_int, _P, c_int64, c_double, _P]),
     "esr_axpy_f64": (c_int, [_P, c_int, _P, c_double, c_int64, _P]),

@@ -12,11 +12,15 @@
 //   Step   :68-76   Ap = A p; alpha = r.z / p.Ap; r -= alpha Ap; x += alpha p
 //   test   :150-153 stop when rnorm <= tol (or the iteration cap)
 //   Update :90-95   z = M r; beta = r.z_new / r.z; p = z + beta p
-// One iteration = three launches (spmv+p.Ap, update+r.r+r.z, p update); each
-// global dot is finished by the last block to arrive, reading the block
-// partials in block order (deterministic, no floating atomics).  The
-// stopping test runs on the device; launches after convergence return at
-// once, so the host can enqueue iterations in chunks and poll.
+// Native precision: three launches per iteration (spmv + p.Ap; update +
+// r.r + r.z; p update).  Mixed precision: two launches per iteration (the p
+// update is folded into the SpMV, recomputing z + beta p for the gathered
+// columns on the FP32 pipes), plus an FP64 true-residual replacement every
+// k iterations.  Every global dot is finished by the last block to arrive,
+// reading the block partials in block order (deterministic, no floating
+// atomics).  The stopping test runs on the device; launches after
+// convergence return at once, so the host can enqueue iterations in chunks
+// and poll.
 #include <cmath>
 #include <cstdint>
 
@@ -26,15 +30,14 @@
 namespace {
 
 constexpr int kCgThreads = 256;
-constexpr int kCgMaxBlocks = 152 * 4;
+constexpr int kCgMaxBlocks = 152 * 8;
 
 struct CgWork {
   esr_cg_scalars s;
-  unsigned int counter[4];
-  double pad_[6];
+  unsigned int counter[8];
   double partial[3][kCgMaxBlocks];
 };
-static_assert(sizeof(esr_cg_scalars) <= 96, "scalars grew");
+static_assert(sizeof(esr_cg_scalars) == 96, "scalars layout");
 
 int cg_blocks(int64_t n) {
   int64_t g = (n + kCgThreads - 1) / kCgThreads;
@@ -45,7 +48,7 @@ int cg_blocks(int64_t n) {
 
 // Dot-product accumulator.  double: FMA in FP64.  float: the product's exact
 // error (fmaf) and a two-sum keep a (hi, lo) pair, i.e. FP64-class
-// accumulation on the FP32 pipes (GB300's FP64 rate is 1/64 of FP32).
+// accumulation on the FP32 pipes (GB300's FP64 rate is 1/59 of FP32).
 template <typename T>
 struct DotAcc;
 template <>
@@ -69,13 +72,10 @@ struct DotAcc<float> {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-struct Sell {
-  int64_t n;
-  const int64_t *slice_ptr;
-  const int32_t *col;
-};
-
-// sum_k x[col]*val in slot order; EXACT: separate rounded mul and add
+// sum_k x[col]*val in slot order; EXACT: separate rounded mul and add.
+// Slices up to 8 slots wide take an unrolled path that issues every column
+// and value load before the dependent gathers (memory-level parallelism);
+// wider slices loop.
 template <typename T, bool EXACT>
 __device__ __forceinline__ T sell_row(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
                                       const int32_t *__restrict__ col, const T *__restrict__ val,
@@ -83,16 +83,37 @@ __device__ __forceinline__ T sell_row(int64_t i, int64_t n, const int64_t *__res
   const int64_t s = i >> 5;
   const int lane = (int)(i & 31);
   const int64_t b = __ldg(slice_ptr + s);
-  const int64_t w = (__ldg(slice_ptr + s + 1) - b) >> 5;
+  const int w = (int)((__ldg(slice_ptr + s + 1) - b) >> 5);
+  const int32_t *cp = col + b + lane;
+  const T *vp = val + b + lane;
   T acc = T(0);
-  for (int64_t k = 0; k < w; ++k) {
-    const int64_t e = b + 32 * k + lane;
-    const int32_t c = __ldg(col + e);
-    if (c >= 0 && (int64_t)c < n) {  // -1 = padding
-      const T v = __ldg(val + e);
+  if (w <= 8) {
+    int32_t c[8];
+    T v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      c[k] = k < w ? __ldg(cp + 32 * k) : -1;
+      v[k] = k < w ? __ldg(vp + 32 * k) : T(0);
+    }
+    T xc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) xc[k] = (c[k] >= 0 && (int64_t)c[k] < n) ? __ldg(x + c[k]) : T(0);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (c[k] >= 0 && (int64_t)c[k] < n) {  // -1 = padding
+        if (EXACT) acc = ops<T>::add(acc, ops<T>::mul(xc[k], v[k]));
+        else acc = fma(xc[k], v[k], acc);
+      }
+    }
+    return acc;
+  }
+  for (int k = 0; k < w; ++k) {
+    const int32_t c = __ldg(cp + 32 * k);
+    if (c >= 0 && (int64_t)c < n) {
+      const T vv = __ldg(vp + 32 * k);
       const T xc = __ldg(x + c);
-      if (EXACT) acc = ops<T>::add(acc, ops<T>::mul(xc, v));
-      else acc = fma(xc, v, acc);
+      if (EXACT) acc = ops<T>::add(acc, ops<T>::mul(xc, vv));
+      else acc = fma(xc, vv, acc);
     }
   }
   return acc;
@@ -136,6 +157,26 @@ __device__ __forceinline__ void finish_two(double a, double b, double *pa, doubl
   tb = esr::block_sum_fixed<kCgThreads>(vb, s_red);
 }
 
+__device__ __forceinline__ void reset_scalars(esr_cg_scalars &s, double bnorm, double rz, double rr, double rtol,
+                                              double atol, int has_atol, int maxiter) {
+  s.bnorm = bnorm;
+  double tol = rtol * s.bnorm;
+  if (has_atol && atol > tol) tol = atol;
+  s.tol = tol;
+  s.rz = rz;
+  s.rz_new = rz;
+  s.rz_prev = rz;
+  s.pq = 0;
+  s.alpha = 0;
+  s.beta = 0;
+  s.rr = rr;
+  s.true_rr = rr;
+  s.iters = 0;
+  s.done = 0;
+  s.maxiter = maxiter;
+  s.replacements = 0;
+}
+
 // ---- init: r = b - A x, z = M r, p = z, b.b, r.z
 template <typename T>
 __global__ void __launch_bounds__(kCgThreads)
@@ -160,25 +201,12 @@ cg_init_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int32_t *
   bool last = false;
   finish_two(bb.value(), rz.value(), w->partial[0], w->partial[1], &w->counter[0], tb, trz, last);
   if (last && threadIdx.x == 0) {
-    esr_cg_scalars &s = w->s;
-    s.bnorm = sqrt(tb);
-    double tol = rtol * s.bnorm;
-    if (has_atol && atol > tol) tol = atol;
-    s.tol = tol;
-    s.rz = trz;
-    s.rz_new = trz;
-    s.pq = 0;
-    s.alpha = 0;
-    s.beta = 0;
-    s.rr = 0;
-    s.iters = 0;
-    s.done = 0;
-    s.maxiter = maxiter;
+    reset_scalars(w->s, sqrt(tb), trz, 0.0, rtol, atol, has_atol, maxiter);
     w->counter[0] = 0u;
   }
 }
 
-// ---- step part 1: q = A p, p.q, alpha = rz / pq
+// ---- step part 1: q = A p, p.q, alpha
 template <typename T>
 __global__ void __launch_bounds__(kCgThreads)
 cg_spmv_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ col,
@@ -204,16 +232,17 @@ cg_spmv_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int32_t *
 }
 
 // ---- step part 2 + update: x += a p; r -= a q; z = M r; r.r; r.z; test
-template <typename T>
+template <typename T, typename XT>
 __global__ void __launch_bounds__(kCgThreads)
-cg_update_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
+cg_update_kernel(int64_t n, XT *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *__restrict__ p,
                  const T *__restrict__ q, const T *__restrict__ invdiag, CgWork *__restrict__ w) {
   if (w->s.done) return;
-  const T a = (T)w->s.alpha;
+  const double ad = w->s.alpha;
+  const T a = (T)ad;
   DotAcc<T> rr, rz;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    x[i] = fma(a, p[i], x[i]);
+    x[i] = fma((XT)ad, (XT)p[i], x[i]);
     const T ri = fma(-a, q[i], r[i]);
     r[i] = ri;
     const T zi = invdiag ? ri * invdiag[i] : ri;
@@ -229,6 +258,7 @@ cg_update_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r, T *__restrict_
     s.iters += 1;
     s.rr = trr;
     s.rz_new = trz;
+    s.rz_prev = s.rz;
     const double rnorm = sqrt(trr);
     if (!isnan(rnorm) && rnorm <= s.tol) {
       s.done = 1;
@@ -244,7 +274,7 @@ cg_update_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r, T *__restrict_
   }
 }
 
-// ---- update part 2: p = z + beta p
+// ---- update part 2 (native path): p = z + beta p
 template <typename T>
 __global__ void __launch_bounds__(kCgThreads)
 cg_pupdate_kernel(int64_t n, const T *__restrict__ z, T *__restrict__ p, const CgWork *__restrict__ w) {
@@ -253,6 +283,86 @@ cg_pupdate_kernel(int64_t n, const T *__restrict__ z, T *__restrict__ p, const C
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     p[i] = fma(beta, p[i], z[i]);
+}
+
+// ---- mixed step part 1: q = A32 p32 on the FP32 pipes (FP32 matrix and an
+// FP32 copy of p for the gathers), p.q accumulated in FP64
+__global__ void __launch_bounds__(kCgThreads)
+cg_spmv_mixed_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ col,
+                     const float *__restrict__ val32, const float *__restrict__ diag32,
+                     const double *__restrict__ p, const float *__restrict__ p32, double *__restrict__ q,
+                     CgWork *__restrict__ w) {
+  if (w->s.done) return;
+  DotAcc<double> pq;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float qf = fmaf(p32[i], diag32[i], sell_row<float, false>(i, n, slice_ptr, col, val32, p32));
+    const double qi = (double)qf;
+    q[i] = qi;
+    pq.add(p[i], qi);
+  }
+  double tpq = 0, unused = 0;
+  bool last = false;
+  finish_two(pq.value(), 0.0, w->partial[0], w->partial[2], &w->counter[1], tpq, unused, last);
+  if (last && threadIdx.x == 0) {
+    w->s.pq = tpq;
+    w->s.alpha = w->s.rz / tpq;
+    w->counter[1] = 0u;
+  }
+}
+
+// ---- mixed update part 2: p = z + beta p, and its FP32 gather copy
+__global__ void __launch_bounds__(kCgThreads)
+cg_pupdate_mixed_kernel(int64_t n, const double *__restrict__ z, double *__restrict__ p, float *__restrict__ p32,
+                        const CgWork *__restrict__ w) {
+  if (w->s.done) return;
+  const double beta = w->s.beta;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double pi = fma(beta, p[i], z[i]);
+    p[i] = pi;
+    p32[i] = (float)pi;
+  }
+}
+
+__global__ void cg_to_f32_kernel(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) b[i] = (float)a[i];
+}
+
+// ---- mixed: the FP64 true residual b - A64 x replaces the recurrence
+// residual (z = M r recomputed, beta rescaled) and decides convergence
+__global__ void __launch_bounds__(kCgThreads)
+cg_replace_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int32_t *__restrict__ col,
+                  const double *__restrict__ val64, const double *__restrict__ diag64, const double *__restrict__ b,
+                  const double *__restrict__ x, double *__restrict__ r, double *__restrict__ z,
+                  const double *__restrict__ invdiag, CgWork *__restrict__ w) {
+  if (w->s.done > 1) return;  // maxiter / breakdown: leave as is
+  DotAcc<double> rr, rz;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double ri = b[i] - fma(x[i], diag64[i], sell_row<double, false>(i, n, slice_ptr, col, val64, x));
+    const double zi = invdiag ? ri * invdiag[i] : ri;
+    r[i] = ri;
+    z[i] = zi;
+    rr.add(ri, ri);
+    rz.add(ri, zi);
+  }
+  double trr = 0, trz = 0;
+  bool last = false;
+  finish_two(rr.value(), rz.value(), w->partial[0], w->partial[1], &w->counter[3], trr, trz, last);
+  if (last && threadIdx.x == 0) {
+    esr_cg_scalars &s = w->s;
+    s.replacements += 1;
+    s.rr = trr;
+    s.true_rr = trr;
+    // rz_prev = r.z before this iteration's update: beta from the true residual
+    if (s.rz_prev != 0.0) s.beta = trz / s.rz_prev;
+    s.rz = trz;
+    const double rnorm = sqrt(trr);
+    s.done = (!isnan(rnorm) && rnorm <= s.tol) ? 1 : 0;
+    w->counter[3] = 0u;
+  }
 }
 
 // ---- true residual ||b - A x|| (exact SpMV, FP64 accumulation)
@@ -271,10 +381,10 @@ true_residual_kernel(int64_t n, const int64_t *__restrict__ slice_ptr, const int
   }
   double t = 0, unused = 0;
   bool last = false;
-  finish_two(rr.value(), 0.0, w->partial[0], w->partial[2], &w->counter[3], t, unused, last);
+  finish_two(rr.value(), 0.0, w->partial[0], w->partial[2], &w->counter[5], t, unused, last);
   if (last && threadIdx.x == 0) {
     *out = sqrt(t);
-    w->counter[3] = 0u;
+    w->counter[5] = 0u;
   }
 }
 
@@ -286,7 +396,15 @@ int check_sell(const esr_sell *A) {
   return ESR_OK;
 }
 
-inline const int64_t *slice_ptr_of(const esr_sell *A) { return A->slice_ptr; }
+int check_pair(const esr_sell *A64, const esr_sell *A32) {
+  int st = check_sell(A64);
+  if (st) return st;
+  if ((st = check_sell(A32))) return st;
+  if (A64->dtype != ESR_F64 || A32->dtype != ESR_F32) return esr::fail(ESR_ERR_ARG, "mixed CG needs an FP64 and an FP32 matrix");
+  if (A64->n != A32->n || A64->nslots != A32->nslots || A64->slice_ptr != A32->slice_ptr || A64->col != A32->col)
+    return esr::fail(ESR_ERR_ARG, "mixed CG: the two matrices must share one SELL layout");
+  return ESR_OK;
+}
 
 }  // namespace
 
@@ -297,12 +415,12 @@ extern "C" int esr_spmv(const esr_sell *A, const void *x, void *y, void *stream)
   if (st) return st;
   if (!x || !y) return esr::fail(ESR_ERR_ARG, "null vector");
   cudaStream_t s = esr::as_stream(stream);
-  const int g = cg_blocks(A->n) * 4 > 152 * 32 ? 152 * 32 : cg_blocks(A->n) * 4;
+  const int g = cg_blocks(A->n);
   if (A->dtype == ESR_F64)
-    spmv_exact_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const double *)A->val,
+    spmv_exact_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const double *)A->val,
                                                        (const double *)A->diag, (const double *)x, (double *)y);
   else
-    spmv_exact_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const float *)A->val,
+    spmv_exact_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const float *)A->val,
                                                       (const float *)A->diag, (const float *)x, (float *)y);
   ESR_LAUNCH_CHECK("esr_spmv");
   return ESR_OK;
@@ -326,12 +444,12 @@ extern "C" int esr_cg_init(const esr_sell *A, const void *b, void *x, void *r, v
   const int g = cg_blocks(A->n);
   const int has_atol = (atol > 0.0) ? 1 : 0;
   if (A->dtype == ESR_F64)
-    cg_init_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const double *)A->val,
+    cg_init_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const double *)A->val,
                                                     (const double *)A->diag, (const double *)b, (const double *)x,
                                                     (double *)r, (double *)z, (double *)p, (const double *)invdiag,
                                                     rtol, atol, has_atol, maxiter, w);
   else
-    cg_init_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const float *)A->val,
+    cg_init_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const float *)A->val,
                                                    (const float *)A->diag, (const float *)b, (const float *)x,
                                                    (float *)r, (float *)z, (float *)p, (const float *)invdiag, rtol,
                                                    atol, has_atol, maxiter, w);
@@ -350,21 +468,59 @@ extern "C" int esr_cg_iterate(const esr_sell *A, void *x, void *r, void *z, void
   const int g = cg_blocks(A->n);
   for (int32_t it = 0; it < k; ++it) {
     if (A->dtype == ESR_F64) {
-      cg_spmv_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const double *)A->val,
+      cg_spmv_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const double *)A->val,
                                                       (const double *)A->diag, (const double *)p, (double *)q, w);
-      cg_update_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, (double *)x, (double *)r, (double *)z,
-                                                        (const double *)p, (const double *)q,
-                                                        (const double *)invdiag, w);
+      cg_update_kernel<double, double><<<g, kCgThreads, 0, s>>>(A->n, (double *)x, (double *)r, (double *)z,
+                                                                (const double *)p, (const double *)q,
+                                                                (const double *)invdiag, w);
       cg_pupdate_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, (const double *)z, (double *)p, w);
     } else {
-      cg_spmv_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const float *)A->val,
+      cg_spmv_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const float *)A->val,
                                                      (const float *)A->diag, (const float *)p, (float *)q, w);
-      cg_update_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, (float *)x, (float *)r, (float *)z, (const float *)p,
-                                                       (const float *)q, (const float *)invdiag, w);
+      cg_update_kernel<float, float><<<g, kCgThreads, 0, s>>>(A->n, (float *)x, (float *)r, (float *)z,
+                                                              (const float *)p, (const float *)q,
+                                                              (const float *)invdiag, w);
       cg_pupdate_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, (const float *)z, (float *)p, w);
     }
   }
   ESR_LAUNCH_CHECK("esr_cg_iterate");
+  return ESR_OK;
+}
+
+extern "C" int esr_cg_mixed_init(const esr_sell *A64, const esr_sell *A32, const double *b, double *x, double *r,
+                                 double *z, double *p, float *p32, const double *invdiag, double rtol, double atol,
+                                 int32_t maxiter, void *workspace, void *stream) {
+  int st = check_pair(A64, A32);
+  if (st) return st;
+  if (!p32) return esr::fail(ESR_ERR_ARG, "null p32");
+  if ((st = esr_cg_init(A64, b, x, r, z, p, invdiag, rtol, atol, maxiter, workspace, stream))) return st;
+  cg_to_f32_kernel<<<cg_blocks(A64->n), kCgThreads, 0, esr::as_stream(stream)>>>(A64->n, p, p32);
+  ESR_LAUNCH_CHECK("esr_cg_mixed_init");
+  return ESR_OK;
+}
+
+extern "C" int esr_cg_mixed_iterate(const esr_sell *A64, const esr_sell *A32, const double *b, double *x, double *r,
+                                    double *z, double *p, float *p32, double *q, const double *invdiag, int32_t k,
+                                    void *workspace, void *stream) {
+  int st = check_pair(A64, A32);
+  if (st) return st;
+  if (!b || !x || !r || !z || !p || !p32 || !q || !workspace) return esr::fail(ESR_ERR_ARG, "null vector");
+  if (k < 1) return esr::fail(ESR_ERR_ARG, "mixed CG iterates in chunks >= 1");
+  cudaStream_t s = esr::as_stream(stream);
+  CgWork *w = (CgWork *)workspace;
+  const int g = cg_blocks(A64->n);
+  for (int32_t it = 0; it < k; ++it) {
+    cg_spmv_mixed_kernel<<<g, kCgThreads, 0, s>>>(A32->n, A32->slice_ptr, A32->col, (const float *)A32->val,
+                                                  (const float *)A32->diag, p, p32, q, w);
+    cg_update_kernel<double, double><<<g, kCgThreads, 0, s>>>(A64->n, x, r, z, p, q, invdiag, w);
+    // the last iteration of the chunk replaces r (and z, beta) by the true
+    // residual before the search direction is updated from them
+    if (it == k - 1)
+      cg_replace_kernel<<<g, kCgThreads, 0, s>>>(A64->n, A64->slice_ptr, A64->col, (const double *)A64->val,
+                                                 (const double *)A64->diag, b, x, r, z, invdiag, w);
+    cg_pupdate_mixed_kernel<<<g, kCgThreads, 0, s>>>(A64->n, z, p, p32, w);
+  }
+  ESR_LAUNCH_CHECK("esr_cg_mixed_iterate");
   return ESR_OK;
 }
 
@@ -386,11 +542,11 @@ extern "C" int esr_true_residual(const esr_sell *A, const void *b, const void *x
   CgWork *w = (CgWork *)workspace;
   const int g = cg_blocks(A->n);
   if (A->dtype == ESR_F64)
-    true_residual_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const double *)A->val,
+    true_residual_kernel<double><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const double *)A->val,
                                                           (const double *)A->diag, (const double *)b,
                                                           (const double *)x, (double *)r, out_f64, w);
   else
-    true_residual_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, slice_ptr_of(A), A->col, (const float *)A->val,
+    true_residual_kernel<float><<<g, kCgThreads, 0, s>>>(A->n, A->slice_ptr, A->col, (const float *)A->val,
                                                          (const float *)A->diag, (const float *)b, (const float *)x,
                                                          (float *)r, out_f64, w);
   ESR_LAUNCH_CHECK("esr_true_residual");

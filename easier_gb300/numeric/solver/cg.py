@@ -124,8 +124,9 @@ class CG(esr.Module):
         """Solve to ``rnorm <= max(rtol*||b||, atol)`` (cg.py:130-161).
 
         ``precision='native'`` iterates in the system's dtype;
-        ``'mixed'`` (FP64 systems) runs FP32-SpMV / FP64-dot CG inside FP64
-        iterative refinement and stops on the FP64 true residual.
+        ``'mixed'`` (FP64 systems) runs the SpMV on FP32 matrix values and an
+        FP32 copy of p, keeps the vectors and dots in FP64, replaces the
+        residual by the FP64 true residual every 32 iterations and stops on it.
         Returns ``{'residual', 'iters'}`` as the reference, plus
         ``'true_residual'`` (||b - A x||, FP64) on the fused path.
         """
@@ -157,12 +158,13 @@ class CG(esr.Module):
         eng = self._fused_solver(precision)
         x, b = self.x.data, self.b.data
         if precision == "mixed":
-            rn, bnorm = eng.solve(b, x, rtol, atol, maxiter)
-            iters = eng.inner_iters
+            s = eng.solve(b, x, self.r.data, self.z.data, self.p.data, rtol, atol, maxiter)
+            rn = float(s.true_rr) ** 0.5
             self.rnorm.data.fill_(rn)
-            self.bnorm.data.fill_(bnorm)
-            info = {"residual": rn, "iters": iters, "true_residual": rn, "outer_iters": eng.outer_iters,
-                    "precision": "mixed"}
+            self.bnorm.data.fill_(s.bnorm)
+            info = {"residual": rn, "iters": max(s.iters - 1, 0), "true_residual": rn,
+                    "replacements": s.replacements, "precision": "mixed",
+                    "status": {1: "converged", 2: "maxiter", 3: "breakdown"}.get(s.done, "?")}
         else:
             s = eng.solve(b, x, self.r.data, self.z.data, self.p.data, rtol, atol, maxiter)
             rnorm = float(s.rr) ** 0.5

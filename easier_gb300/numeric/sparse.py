@@ -144,50 +144,67 @@ class FusedPCG:
 
 
 class MixedPCG:
-    """FP32-SpMV / FP64-dot CG inside FP64 iterative refinement.
+    """FP32-SpMV / FP64-vector PCG with FP64 true-residual replacement.
 
-    Outer loop (FP64): r = b - A64 x (exact FP64 SpMV, the true residual);
-    stop when ||r|| <= tol.  Inner: FP32 Jacobi-PCG on A32 d = r/||r|| with
-    FP64-class dot accumulation, to `inner_rtol`; then x += ||r|| * d.
+    The SpMV runs on the FP32 pipes (FP32 matrix values and an FP32 copy of
+    the search direction for the gathers); x, r, z, p, q and every dot
+    product stay FP64 (an FP32 recurrence loses too much at the conditioning
+    of these systems), and after every chunk of iterations the FP64 true
+    residual b - A64 x replaces r (the search direction is kept, so CG does
+    not restart) and decides convergence.
     """
 
-    def __init__(self, A64: SellMatrix, jacobi: bool = True, inner_rtol: float = 1e-3, chunk: int = 32,
-                 use_graph: bool = True):
+    def __init__(self, A64: SellMatrix, jacobi: bool = True, chunk: int = 32, use_graph: bool = True):
         self.A64 = A64
         self.A32 = A64.astype(torch.float32)
-        self.inner = FusedPCG(self.A32, jacobi=jacobi, chunk=chunk, use_graph=use_graph)
-        self.outer = FusedPCG(A64, jacobi=False, chunk=chunk, use_graph=False)
         n, dev = A64.n, A64.device
-        self.r64 = torch.empty(n, dtype=torch.float64, device=dev)
-        self.rhs32 = torch.empty(n, dtype=torch.float32, device=dev)
-        self.d32 = torch.empty(n, dtype=torch.float32, device=dev)
-        self.r32 = torch.empty(n, dtype=torch.float32, device=dev)
-        self.z32 = torch.empty(n, dtype=torch.float32, device=dev)
+        self.n, self.dev = n, dev
+        self.invdiag = (1.0 / A64.diag).contiguous() if jacobi else None
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.q = torch.empty(n, **f64)
         self.p32 = torch.empty(n, dtype=torch.float32, device=dev)
-        self.inner_rtol = inner_rtol
-        self.inner_iters = 0
-        self.outer_iters = 0
+        self.ws = torch.zeros(int(_lib.lib().esr_cg_workspace_bytes(n)), dtype=torch.uint8, device=dev)
+        self.chunk = chunk
+        self.use_graph = use_graph
+        self._graphs = {}
+        self.kernel_launches = 0
 
-    def solve(self, b, x, rtol: float, atol: Optional[float], maxiter: Optional[int]):
-        dev = self.A64.device
-        stream = _lib.stream_handle(dev)
-        bnorm = float(torch.linalg.vector_norm(b).item())
-        tol = rtol * bnorm
-        if atol and atol > tol:
-            tol = atol
-        self.inner_iters = 0
-        self.outer_iters = 0
-        budget = None if maxiter is None else int(maxiter)
-        while True:
-            rn = self.outer.true_residual(b, x, self.r64)
-            if rn <= tol or (budget is not None and self.inner_iters >= budget) or not np.isfinite(rn):
-                return rn, bnorm
-            self.outer_iters += 1
-            _lib.call("esr_convert", _lib.F64, _lib.ptr(self.r64), _lib.F32, _lib.ptr(self.rhs32), self.A64.n,
-                      1.0 / rn, stream)
-            self.d32.zero_()
-            inner_tol = max(self.inner_rtol, 0.5 * tol / rn)
-            left = None if budget is None else max(budget - self.inner_iters, 0)
-            s = self.inner.solve(self.rhs32, self.d32, self.r32, self.z32, self.p32, inner_tol, None, left)
-            self.inner_iters += s.iters
-            _lib.call("esr_axpy_f64", _lib.ptr(x), _lib.F32, _lib.ptr(self.d32), rn, self.A64.n, stream)
+    def _iterate_call(self, b, x, r, z, p):
+        _lib.call("esr_cg_mixed_iterate", ctypes.byref(self.A64.desc), ctypes.byref(self.A32.desc), _lib.ptr(b),
+                  _lib.ptr(x), _lib.ptr(r), _lib.ptr(z), _lib.ptr(p), _lib.ptr(self.p32), _lib.ptr(self.q),
+                  _lib.ptr(self.invdiag), int(self.chunk), _lib.ptr(self.ws), _lib.stream_handle(self.dev))
+
+    def _chunk(self, b, x, r, z, p):
+        if not self.use_graph:
+            self._iterate_call(b, x, r, z, p)
+            return
+        key = (b.data_ptr(), x.data_ptr(), r.data_ptr(), z.data_ptr(), p.data_ptr())
+        g = self._graphs.get(key)
+        if g is None:
+            s = torch.cuda.Stream(self.dev)
+            s.wait_stream(torch.cuda.current_stream(self.dev))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self._iterate_call(b, x, r, z, p)
+            torch.cuda.current_stream(self.dev).wait_stream(s)
+            self._graphs[key] = g
+        g.replay()
+
+    def scalars(self) -> _lib.CgScalars:
+        out = _lib.CgScalars()
+        _lib.call("esr_cg_read_scalars", _lib.ptr(self.ws), ctypes.byref(out), _lib.stream_handle(self.dev))
+        return out
+
+    def solve(self, b, x, r, z, p, rtol: float, atol: Optional[float], maxiter: Optional[int]) -> _lib.CgScalars:
+        _lib.call("esr_cg_mixed_init", ctypes.byref(self.A64.desc), ctypes.byref(self.A32.desc), _lib.ptr(b),
+                  _lib.ptr(x), _lib.ptr(r), _lib.ptr(z), _lib.ptr(p), _lib.ptr(self.p32), _lib.ptr(self.invdiag),
+                  float(rtol), float(atol) if atol else 0.0, -1 if maxiter is None else int(maxiter),
+                  _lib.ptr(self.ws), _lib.stream_handle(self.dev))
+        self.kernel_launches += 2
+        s = self.scalars()
+        while not s.done:
+            self._chunk(b, x, r, z, p)
+            self.kernel_launches += 3 * self.chunk + 1
+            s = self.scalars()
+        return s

@@ -366,10 +366,12 @@ typedef struct {
   double bnorm;
   double tol;      /* absolute stopping tolerance on ||r||           */
   double rz_new;
+  double rz_prev;  /* r.z before the last update (for replacements)  */
+  double true_rr;  /* ||b - A x||^2 at the last replacement (mixed)  */
   int32_t iters;   /* completed step() calls                        */
   int32_t done;    /* 1 = converged, 2 = maxiter, 3 = breakdown/NaN  */
   int32_t maxiter; /* < 0: unlimited                                 */
-  int32_t pad_;
+  int32_t replacements; /* true-residual replacements (mixed)        */
 } esr_cg_scalars;
 
 /* PCG set-up (easier/numeric/solver/cg.py:49-53 Init + :136-139):
@@ -390,6 +392,26 @@ int esr_cg_iterate(const esr_sell *A, void *x, void *r, void *z, void *p,
 /* Copy the device scalars to host memory (synchronises `stream`). */
 int esr_cg_read_scalars(const void *workspace, esr_cg_scalars *out,
                         void *stream);
+
+/* Mixed-precision PCG: the SpMV runs on the FP32 pipes (FP32 matrix values
+ * A32 and an FP32 copy p32 of the search direction for the gathers), the
+ * vectors x, r, z, p, q and every dot product stay FP64, and after every
+ * chunk of k iterations the FP64 true residual b - A64 x replaces r (the
+ * search direction is kept: no restart) and decides convergence, so a
+ * converged solve is FP64-verified.  A64/A32 share one SELL layout.
+ * No reference counterpart (the reference CG is FP64 only). */
+int esr_cg_mixed_init(const esr_sell *A64, const esr_sell *A32, const double *b,
+                      double *x, double *r, double *z, double *p, float *p32,
+                      const double *invdiag, double rtol, double atol,
+                      int32_t maxiter, void *workspace, void *stream);
+
+/* `k` (>= 1) mixed iterations followed by one true-residual replacement;
+ * iterations after convergence are no-ops. */
+int esr_cg_mixed_iterate(const esr_sell *A64, const esr_sell *A32,
+                         const double *b, double *x, double *r, double *z,
+                         double *p, float *p32, double *q,
+                         const double *invdiag, int32_t k, void *workspace,
+                         void *stream);
 
 /* ||b - A x||_2 in FP64 (true residual); out_f64 on the device.
  * `r` is scratch of length n (receives b - A x). */

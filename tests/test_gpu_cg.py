@@ -111,7 +111,7 @@ def test_mixed_precision_reaches_fp64_true_residual():
     s = mesh.p1_system(96)
     tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, b, eqn.x.collect().cpu().numpy())
     assert tr <= 1e-8 * np.linalg.norm(b)
-    assert info["outer_iters"] >= 2
+    assert info["replacements"] >= 1 and info["status"] == "converged"
     eqn.x.data.zero_()
     info64 = sol.solve(rtol=1e-8)
     x64 = eqn.x.collect().cpu().numpy()
