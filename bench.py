@@ -11,7 +11,12 @@ Workloads (``--workload``):
   poisson  P1 Poisson, 1000x1000 grid (998,001 unknowns, 5,980,016 directed
            couplings), random-mode RHS, Jacobi-PCG to relative residual 1e-8;
            one bench step = one solve; metric solves/s
-           (``--precision native|mixed``).
+           (``--precision native|mixed|df64``).
+  batched  256 P1 Poisson instances, side N ~ U{32..512} (seeded), GRF
+           kappa, random-mode RHS, packed block-diagonal, lockstep
+           Jacobi-PCG per instance to FP64-verified relative residual 1e-8;
+           one bench step = one batch solve; metric solves/s
+           (``--precision df64|fp64``).
 
 ``--impl reference`` times the oracle (the reference's CPU algorithm, the
 same aten ops its CPU backend runs) on this machine's host cores, on a
@@ -343,25 +348,148 @@ def bench_poisson(args, world, rank, local):
         raise RuntimeError(f"true relative residual {rel:.3e} above 1e-8")
     nit = statistics.mean(iters)
     eng = sol._fused
-    A = eng.A if hasattr(eng, "A") else eng.A64
-    s = A.val.element_size()
-    bytes_it = A.col.numel() * (4 + s) + A.n * (8 + 2 * s) + A.n * 12 * s
+    if hasattr(eng, "bytes_per_iteration"):
+        bytes_it = eng.bytes_per_iteration()
+    else:
+        bytes_it = eng.bytes_per_row_iteration() * eng.pack.n
     achieved = bytes_it * nit / (ms / args.steps / 1e3) / 1e9
+    dtype = {"native": "f64", "mixed": "f32-spmv/f64-dot", "df64": "df64 (f32 pairs)"}[args.precision]
     peak, peak_kind = _peaks()
     line = {
         "metric": "Poisson solves/s", "value": world * args.steps / (ms / 1e3), "unit": "solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "native" else "f32-spmv/f64-dot",
+        "dtype": dtype,
         "data": "synthetic (16 random sine modes, seed 0)",
         "config": {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to FP64 true rel. residual 1e-8",
-                   "unknowns": A.n, "couplings": int(A.nnz), "iterations": nit, "precision": args.precision,
+                   "unknowns": eqn.nunk, "couplings": int(eqn.selector.idx.numel()), "iterations": nit,
+                   "precision": args.precision, "bytes_per_iteration": bytes_it,
                    "true_rel_residual": rel, "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None},
         "gpu_launches": int(eng.kernel_launches if hasattr(eng, "kernel_launches") else 0),
         "clocks": clk.summary(),
     }
+    return line
+
+
+# -------------------------------------------------------- batched Poisson --
+def batched_cpu_baseline(insts, iters, budget_s=20.0, count=16):
+    """Oracle Jacobi-PCG on a seeded subset of the instances, each run for a
+    bounded number of iterations; the per-(unknown x iteration) cost is
+    scaled by every instance's iteration count from the GPU run."""
+    from oracle import cg as ocg
+    rng = np.random.default_rng(0)
+    pick = rng.choice(len(insts), size=min(count, len(insts)), replace=False)
+    work, wall = 0.0, 0.0
+    per = max(1.0, budget_s / len(pick))
+    for i in pick:
+        s = insts[i]
+        k = 10
+        while True:
+            t0 = time.perf_counter()
+            ocg.cg(s.row, s.col, s.Ae, s.Av, s.b, rtol=0.0, maxiter=k - 1, jacobi=True)
+            dt = time.perf_counter() - t0
+            if dt >= 0.25 * per or k >= iters[i] + 1:
+                break
+            k *= 4
+        work += k * s.n
+        wall += dt
+    cost = wall / work
+    total = sum((it + 1) * s.n for it, s in zip(iters, insts)) * cost
+    sizes = sorted(int(round(np.sqrt(insts[i].n))) + 1 for i in pick)
+    return len(insts) / total, (f"oracle Jacobi-PCG on {len(pick)} seeded instances (N={sizes}), bounded iterations, "
+                                f"{cost * 1e9:.2f} ns per unknown-iteration scaled by the {len(insts)} instances' "
+                                f"iteration counts")
+
+
+def bench_batched(args, world, rank, local):
+    from easier_gb300.numeric.batched import BatchedPCG, p1_instances
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    prec = "fp64" if args.precision in ("native", "fp64") else "df64"
+    t0 = time.perf_counter()
+    insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
+    eng = BatchedPCG(insts, jacobi=True, precision=prec, device=dev, graph_iters=args.chunk)
+    prep = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tuning = eng.autotune() if not args.no_autotune else None
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    x_start = torch.zeros_like(eng.b64)
+    for _ in range(args.warmup):
+        eng.load_packed(x0=x_start)
+        eng.run(1e-8)
+    torch.cuda.synchronize(dev)
+    launches0 = eng.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        _barrier(world)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            eng.load_packed(x0=x_start)
+            eng.run(1e-8)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        _barrier(world)
+    ms = _max_over_ranks(world, e0.elapsed_time(e1))
+    launches = (eng.kernel_launches - launches0) // args.steps
+    res = [eng._info(s) for s in eng.instances()]
+    bad = [i for i, r in enumerate(res) if r["status"] != "converged" or not r["true_residual"] <= 1e-8 * r["bnorm"]
+           * 1.0001]
+    if bad:
+        raise RuntimeError(f"{len(bad)} instances not FP64-verified at rel. residual 1e-8, e.g. {res[bad[0]]}")
+    iters = [r["iters"] for r in res]
+    pk = eng.pack
+    npad = np.diff(pk.inst_block0.astype(np.int64)) * 256
+    row_its = float(sum((it + 1 + r["restarts"]) * n for it, r, n in zip(iters, res, npad)))
+    bytes_solve = row_its * eng.bytes_per_row_iteration()
+    sec = ms / args.steps / 1e3
+    achieved = bytes_solve / sec / 1e9
+    peak, peak_kind = _peaks()
+    # end to end: packed right hand sides from pinned host memory in, FP64
+    # solutions back to pinned host memory, every step
+    b_host = eng.b64.cpu().pin_memory()
+    x_host = torch.empty(pk.n, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        eng.load_packed(b64=b_host.to(dev, non_blocking=True), x0=x_start)
+        eng.run(1e-8)
+        x_host.copy_(eng.solution(), non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e2e_sec = (time.perf_counter() - t0) / e2e_steps
+    line = {
+        "metric": "Poisson solves/s (batched)", "value": world * pk.ninst / sec, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == "fp64" else "df64 (f32 pairs)",
+        "data": f"synthetic (seed {args.seed}: GRF kappa corr. 0.1 var 1, 16 random sine modes)",
+        "config": {"workload": f"batched P1 Poisson, {pk.ninst} instances, N ~ U{{{args.nmin}..{args.nmax}}}, "
+                               f"Jacobi-PCG per instance to FP64 true rel. residual 1e-8",
+                   "unknowns": int(pk.sizes.sum()), "packed_rows": pk.n, "stored_slots": int(pk.slice_ptr[-1]),
+                   "iterations_max": max(iters), "iterations_mean": float(np.mean(iters)),
+                   "restarts": int(sum(r["restarts"] for r in res)), "precision": prec,
+                   "graph_iters": eng.graph_iters, "tiles_per_chunk": eng.tiles_per_chunk, "grid": eng.grid,
+                   "autotune": None if tuning is None else
+                   {"s": tune_s, "ms_per_iter_all_running": tuning["ms_per_iter"],
+                    "candidates": len(tuning["table"])},
+                   "setup_s": prep, "inputs_vs_l2": "working set > L2 (vectors alone > 1 GB)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "bytes_per_row_iteration": eng.bytes_per_row_iteration()},
+        "e2e": {"value": world * pk.ninst / e2e_sec, "unit": "solves/s", "h2d_bytes_per_step": pk.n * 8,
+                "d2h_bytes_per_step": pk.n * 8},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, sample = batched_cpu_baseline(insts, iters)
+        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": sample}
     return line
 
 
@@ -388,6 +516,27 @@ def bench_reference(args):
         unit, metric = "cell-steps/s", "SWE cell-steps/s"
         sample = f"{args.steps} full oracle steps at N={args.n} ({m.nc} cells), {args.dtype}"
         cfg = {"workload": f"shallow water, tutorial mesh N={args.n} ({m.nc} cells, {m.ne} directed edges), dt={args.dt}"}
+    elif args.workload == "batched":
+        from easier_gb300.numeric.batched import p1_instances
+        from oracle import cg as ocg
+        insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
+        order = np.random.default_rng(0).permutation(len(insts))
+        for i in order[:args.warmup]:
+            s = insts[i]
+            ocg.cg(s.row, s.col, s.Ae, s.Av, s.b, rtol=1e-8, jacobi=True)
+        sizes = []
+        t0 = time.perf_counter()
+        for i in order[args.warmup:args.warmup + args.steps]:
+            s = insts[i]
+            ocg.cg(s.row, s.col, s.Ae, s.Av, s.b, rtol=1e-8, jacobi=True)
+            sizes.append(int(round(np.sqrt(s.n))) + 1)
+        wall = time.perf_counter() - t0
+        v = args.steps / wall
+        unit, metric = "solves/s", "Poisson solves/s (batched)"
+        sample = (f"{args.steps} full Jacobi-PCG solves of seeded instances drawn from the batch "
+                  f"(N={sizes}), one per step")
+        cfg = {"workload": f"batched P1 Poisson, {args.count} instances, N ~ U{{{args.nmin}..{args.nmax}}}, "
+                           f"Jacobi-PCG per instance to rel. residual 1e-8"}
     else:
         from easier_gb300 import mesh
         from oracle import cg as ocg
@@ -417,11 +566,17 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["swe", "poisson"], default="swe")
+    ap.add_argument("--workload", choices=["swe", "poisson", "batched"], default="swe")
+    ap.add_argument("--count", type=int, default=256, help="batched: instances")
+    ap.add_argument("--nmin", type=int, default=32, help="batched: smallest mesh side")
+    ap.add_argument("--nmax", type=int, default=512, help="batched: largest mesh side")
+    ap.add_argument("--seed", type=int, default=0, help="batched: instance seed")
+    ap.add_argument("--chunk", type=int, default=32, help="batched: iterations per CUDA graph")
+    ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default work shape")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
     ap.add_argument("--dt", type=float, default=None)
-    ap.add_argument("--precision", choices=["native", "mixed", "exact", "fast"], default=None)
+    ap.add_argument("--precision", choices=["native", "mixed", "df64", "fp64", "exact", "fast"], default=None)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -439,15 +594,15 @@ def main():
     world, rank, local = _dist()
     if args.impl == "reference":
         if args.steps is None:
-            args.steps = 3 if args.workload == "swe" else 1
+            args.steps = {"swe": 3, "poisson": 1, "batched": 4}[args.workload]
         if args.warmup is None:
-            args.warmup = 1 if args.workload == "swe" else 0
+            args.warmup = {"swe": 1, "poisson": 0, "batched": 1}[args.workload]
         if rank != 0:
             return
         print(json.dumps(bench_reference(args)), flush=True)
         return
     if args.steps is None:
-        args.steps = 1000 if args.workload == "swe" else 10
+        args.steps = {"swe": 1000, "poisson": 10, "batched": 5}[args.workload]
     if args.warmup is None:
         args.warmup = 10 if args.workload == "swe" else 3
     if args.warmup < 3:
@@ -455,7 +610,8 @@ def main():
     if world > 1:
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    line = bench_swe(args, world, rank, local) if args.workload == "swe" else bench_poisson(args, world, rank, local)
+    run = {"swe": bench_swe, "poisson": bench_poisson, "batched": bench_batched}[args.workload]
+    line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

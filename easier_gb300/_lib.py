@@ -50,6 +50,21 @@ class CgScalars(Structure):
                 ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("replacements", c_int32)]
 
 
+class Batch(Structure):
+    _fields_ = [("n", c_int64), ("ninst", c_int32), ("nblocks", c_int32), ("rows_per_block", c_int32),
+                ("df64", c_int32), ("nchunks", c_int32), ("grid", c_int32), ("slice_ptr", c_void_p),
+                ("col", c_void_p), ("val", c_void_p), ("diag", c_void_p), ("invdiag", c_void_p),
+                ("val64", c_void_p), ("diag64", c_void_p), ("block_inst", c_void_p), ("inst_block0", c_void_p),
+                ("chunk_tile0", c_void_p), ("chunk_inst", c_void_p), ("inst_chunk0", c_void_p)]
+
+
+class BcgInst(Structure):
+    _fields_ = [("rz", c_double), ("pq", c_double), ("alpha", c_double), ("beta", c_double),
+                ("rr", c_double), ("bnorm", c_double), ("tol", c_double), ("true_rr", c_double),
+                ("iters", c_int32), ("done", c_int32), ("verified", c_int32), ("restarts", c_int32),
+                ("maxiter", c_int32), ("pad_", c_int32)]
+
+
 _P = c_void_p
 _SIGS = {
     "esr_last_error": (c_char_p, []),
@@ -91,9 +106,14 @@ _SIGS = {
     "esr_true_residual": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P]),
     "esr_convert": (c_int, [c_int, _P, c_int, _P, c_int64, c_double, _P]),
     "esr_axpy_f64": (c_int, [_P, c_int, _P, c_double, c_int64, _P]),
+    "esr_bcg_workspace_bytes": (c_int64, [c_int32, c_int32, c_int32]),
+    "esr_bcg_init": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, c_double, c_double, c_int32, _P, _P]),
+    "esr_bcg_iterate": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, c_int32, _P, _P]),
+    "esr_bcg_verify": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "esr_bcg_status": (c_int, [_P, c_int32, c_int32, POINTER(c_int32), POINTER(BcgInst), _P]),
 }
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 
 def library_path() -> Path:

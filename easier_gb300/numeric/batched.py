@@ -1,0 +1,397 @@
+"""Batched (P)CG: many independent ``Linsys`` instances solved in lockstep.
+
+The instances are packed as one block-diagonal SELL-32 system.  Each
+instance's rows are padded to a multiple of 256 (identity rows, zero right
+hand side), so every 256-row CTA of the device kernels belongs to exactly one
+instance and every per-instance dot product is finished by the last CTA of
+that instance (``include/esr_gb300.h``, ``esr_bcg_*``).  Per instance the
+iteration and stopping test are those of easier/numeric/solver/cg.py:68-161
+(Jacobi ``M`` or none).  Converged instances are re-checked on the FP64 true
+residual ``b - A x``; an instance that fails restarts from it.
+
+Two arithmetic precisions:
+
+``"fp64"``  FP64 matrix, vectors and dots (the reference's precision);
+``"df64"``  double-float pairs (two FP32 numbers per value, ~48 significand
+            bits) for the matrix, vectors and dots, on the FP32 pipes, with the
+            FP64 true residual deciding convergence.
+
+A single system is a batch of one (``CG.solve(precision="df64")``).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from .. import _lib, mesh
+
+ROWS_PER_BLOCK = 256
+STATUS = {0: "running", 1: "converged", 2: "maxiter", 3: "breakdown"}
+
+
+@dataclass
+class LinsysInstance:
+    """One system in Linsys form: A x = reducer(x[col] * Ae) + x * Av with the
+    Reducer index ``row``; ``b`` the right hand side, ``x0`` the start (zero
+    when None).  Arrays are numpy or torch (any device)."""
+    n: int
+    row: np.ndarray
+    col: np.ndarray
+    Ae: object
+    Av: object
+    b: object
+    x0: object = None
+
+
+def _np(a, dtype):
+    if isinstance(a, torch.Tensor):
+        a = a.detach().cpu().numpy()
+    return np.ascontiguousarray(np.asarray(a, dtype=dtype))
+
+
+def split_df64(t: torch.Tensor) -> torch.Tensor:
+    """FP64 tensor -> [..., 2] FP32 pairs (hi, lo) with hi + lo == t to ~48 bits."""
+    t = t.to(torch.float64)
+    hi = t.to(torch.float32)
+    lo = (t - hi.to(torch.float64)).to(torch.float32)
+    return torch.stack([hi, lo], dim=-1).contiguous()
+
+
+def join_df64(t: torch.Tensor) -> torch.Tensor:
+    return t[..., 0].to(torch.float64) + t[..., 1].to(torch.float64)
+
+
+class PackedBatch:
+    """Host packing of instances into one block-diagonal SELL-32 system.
+
+    Slices never span instances (256-row blocks, 32-row slices), so each
+    instance's SELL layout is built on its own and the layouts concatenated
+    with row/slot offsets.  Entries of a row keep the reference's edge order
+    (stable sort of the Reducer index)."""
+
+    def __init__(self, instances: Sequence[LinsysInstance]):
+        if len(instances) == 0:
+            raise ValueError("empty batch")
+        nblk = [max(1, -(-int(s.n) // ROWS_PER_BLOCK)) for s in instances]
+        self.ninst = len(instances)
+        self.sizes = np.array([int(s.n) for s in instances], np.int64)
+        self.inst_block0 = np.zeros(self.ninst + 1, np.int32)
+        self.inst_block0[1:] = np.cumsum(nblk)
+        self.nblocks = int(self.inst_block0[-1])
+        self.n = self.nblocks * ROWS_PER_BLOCK
+        self.row0 = self.inst_block0[:-1].astype(np.int64) * ROWS_PER_BLOCK
+        self.block_inst = np.repeat(np.arange(self.ninst, dtype=np.int32), nblk)
+        sp_parts, col_parts, val_parts = [], [], []
+        self.diag = np.ones(self.n, np.float64)
+        self.b = np.zeros(self.n, np.float64)
+        self.x0 = np.zeros(self.n, np.float64)
+        base = 0
+        for i, s in enumerate(instances):
+            n, r0, npad = int(s.n), int(self.row0[i]), nblk[i] * ROWS_PER_BLOCK
+            row, col = _np(s.row, np.int64), _np(s.col, np.int64)
+            Ae, Av = _np(s.Ae, np.float64), _np(s.Av, np.float64)
+            if row.shape != col.shape or row.shape != Ae.shape or Av.shape != (n,):
+                raise ValueError(f"instance {i}: inconsistent Linsys arrays")
+            rowptr, perm = mesh.csr_from_index(row, npad)
+            slice_ptr, c, src_pos = mesh.sell_layout(npad, rowptr, perm, col, n)
+            valid = src_pos >= 0
+            val = np.where(valid, Ae[np.where(valid, src_pos, 0)], 0.0)
+            sp_parts.append(slice_ptr[:-1] + base)
+            col_parts.append(np.where(c >= 0, c + r0, -1).astype(np.int32))
+            val_parts.append(val)
+            base += int(slice_ptr[-1])
+            self.diag[r0:r0 + n] = Av
+            self.b[r0:r0 + n] = _np(s.b, np.float64)
+            if s.x0 is not None:
+                self.x0[r0:r0 + n] = _np(s.x0, np.float64)
+        if self.n >= 2 ** 31:
+            raise ValueError("batch too large for int32 column indices")
+        self.slice_ptr = np.concatenate(sp_parts + [np.array([base], np.int64)])
+        self.col = np.concatenate(col_parts)
+        self.val = np.concatenate(val_parts)
+
+    def rows(self, i: int) -> slice:
+        r0 = int(self.row0[i])
+        return slice(r0, r0 + int(self.sizes[i]))
+
+
+def chunk_layout(inst_block0: np.ndarray, tiles_per_chunk: int):
+    """Chunks of up to ``tiles_per_chunk`` consecutive tiles of one instance:
+    chunk_tile0 [nchunks+1], chunk_inst [nchunks], inst_chunk0 [ninst+1]."""
+    m = int(tiles_per_chunk)
+    if m < 1:
+        raise ValueError("tiles_per_chunk must be >= 1")
+    ntiles = np.diff(inst_block0.astype(np.int64))
+    nch = -(-ntiles // m)
+    inst_chunk0 = np.zeros(len(ntiles) + 1, np.int64)
+    inst_chunk0[1:] = np.cumsum(nch)
+    chunk_inst = np.repeat(np.arange(len(ntiles), dtype=np.int64), nch)
+    j = np.arange(int(inst_chunk0[-1])) - inst_chunk0[chunk_inst]
+    chunk_tile0 = np.empty(int(inst_chunk0[-1]) + 1, np.int64)
+    chunk_tile0[:-1] = inst_block0[chunk_inst].astype(np.int64) + j * m
+    chunk_tile0[-1] = int(inst_block0[-1])
+    return chunk_tile0.astype(np.int32), chunk_inst.astype(np.int32), inst_chunk0.astype(np.int32)
+
+
+class BatchedPCG:
+    """Lockstep (P)CG over a packed batch on one GPU.
+
+    ``run`` enqueues iterations in groups of up to ``graph_iters``, each group
+    one CUDA graph (1 compaction + 3 persistent launches per iteration);
+    between groups the host reads the 4-byte running-instance counter.
+    The work shape -- 256-row tiles per CTA work unit (``tiles_per_chunk``)
+    and persistent CTAs (``grid``) -- is set by ``autotune`` or by hand."""
+
+    def __init__(self, instances: Sequence[LinsysInstance], jacobi: bool = True, precision: str = "df64",
+                 device="cuda", graph_iters: int = 32, use_graph: bool = True, tiles_per_chunk: int = 4,
+                 grid: Optional[int] = None):
+        if precision not in ("fp64", "df64"):
+            raise ValueError("precision must be 'fp64' or 'df64'")
+        dev = torch.device(device)
+        if dev.type != "cuda":
+            raise ValueError("BatchedPCG runs on a CUDA device")
+        pk = PackedBatch(instances)
+        self.pack = pk
+        self.dev = dev
+        self.precision = precision
+        self.graph_iters = int(graph_iters)
+        self.use_graph = use_graph
+        self.jacobi = jacobi
+        n = pk.n
+        t = lambda a: torch.from_numpy(a).to(dev)
+        self.slice_ptr = t(pk.slice_ptr)
+        self.col = t(pk.col)
+        self.block_inst = t(pk.block_inst)
+        self.inst_block0 = t(pk.inst_block0)
+        self.val64 = t(pk.val)
+        self.diag64 = t(pk.diag)
+        self.b64 = t(pk.b)
+        inv64 = (1.0 / self.diag64) if jacobi else None
+        df = precision == "df64"
+        conv = split_df64 if df else (lambda a: a.contiguous())
+        self.val = conv(self.val64)
+        self.diag = conv(self.diag64)
+        self.invdiag = conv(inv64) if jacobi else None
+        self.b = conv(self.b64)
+        self.x = conv(t(pk.x0))
+        self.r, self.z, self.p, self.q = (torch.zeros_like(self.x) for _ in range(4))
+        self.x64 = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.r64 = torch.zeros(n, dtype=torch.float64, device=dev)
+        # sized for the finest chunking (one tile per chunk)
+        nbytes = int(_lib.lib().esr_bcg_workspace_bytes(pk.ninst, pk.nblocks, pk.nblocks))
+        self.ws = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
+        self.sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        self._graphs = {}
+        self.kernel_launches = 0
+        self.polls = 0
+        self.tuning = None
+        self.set_shape(tiles_per_chunk, grid if grid is not None else 4 * self.sm_count)
+
+    def set_shape(self, tiles_per_chunk: int, grid: int):
+        """Work unit of the persistent kernels (tiles per chunk) and their
+        CTA count."""
+        ct0, cinst, ic0 = chunk_layout(self.pack.inst_block0, tiles_per_chunk)
+        self.tiles_per_chunk = int(tiles_per_chunk)
+        self.grid = int(grid)
+        self.nchunks = len(cinst)
+        self.chunk_tile0 = torch.from_numpy(ct0).to(self.dev)
+        self.chunk_inst = torch.from_numpy(cinst).to(self.dev)
+        self.inst_chunk0 = torch.from_numpy(ic0).to(self.dev)
+        pk = self.pack
+        self.desc = _lib.Batch(pk.n, pk.ninst, pk.nblocks, ROWS_PER_BLOCK, 1 if self.precision == "df64" else 0,
+                               self.nchunks, self.grid, _lib.ptr(self.slice_ptr), _lib.ptr(self.col),
+                               _lib.ptr(self.val), _lib.ptr(self.diag), _lib.ptr(self.invdiag),
+                               _lib.ptr(self.val64), _lib.ptr(self.diag64), _lib.ptr(self.block_inst),
+                               _lib.ptr(self.inst_block0), _lib.ptr(self.chunk_tile0), _lib.ptr(self.chunk_inst),
+                               _lib.ptr(self.inst_chunk0))
+        self._graphs = {}
+
+    def bytes_per_row_iteration(self) -> float:
+        """Algorithmic HBM bytes of one lockstep iteration per active packed
+        row (8-byte values in both precisions): SpMV streams col and val
+        (per stored slot), diag, gathers p, writes q; the update reads x, r,
+        p, q, invdiag and writes x, r, z; the p-update reads z, p, writes p."""
+        slots = self.pack.slice_ptr[-1] / self.pack.n
+        return slots * 12 + 8 * 14 + 8 / 32
+
+    def load_packed(self, b64: Optional[torch.Tensor] = None, x0: Optional[torch.Tensor] = None):
+        """Replace the packed right hand side and/or start vector (FP64,
+        length n, padding rows zero)."""
+        conv = split_df64 if self.precision == "df64" else (lambda a: a)
+        if b64 is not None:
+            self.b64.copy_(b64)
+            self.b.copy_(conv(self.b64))
+        if x0 is not None:
+            self.x.copy_(conv(x0.to(self.dev, torch.float64)))
+
+    # ------------------------------------------------------------- calls --
+    def _stream(self):
+        return _lib.stream_handle(self.dev)
+
+    def _iterate_call(self, k: int):
+        _lib.call("esr_bcg_iterate", ctypes.byref(self.desc), _lib.ptr(self.x), _lib.ptr(self.r), _lib.ptr(self.z),
+                  _lib.ptr(self.p), _lib.ptr(self.q), int(k), _lib.ptr(self.ws), self._stream())
+
+    def _group(self, k: int):
+        self.kernel_launches += 1 + 3 * k
+        if not self.use_graph:
+            self._iterate_call(k)
+            return
+        g = self._graphs.get(k)
+        if g is None:
+            s = torch.cuda.Stream(self.dev)
+            s.wait_stream(torch.cuda.current_stream(self.dev))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self._iterate_call(k)
+            torch.cuda.current_stream(self.dev).wait_stream(s)
+            self._graphs[k] = g
+        g.replay()
+
+    def active(self) -> int:
+        a = ctypes.c_int32()
+        _lib.call("esr_bcg_status", _lib.ptr(self.ws), self.pack.ninst, self.nchunks, ctypes.byref(a), None,
+                  self._stream())
+        self.polls += 1
+        return int(a.value)
+
+    def instances(self) -> List[_lib.BcgInst]:
+        a = ctypes.c_int32()
+        out = (_lib.BcgInst * self.pack.ninst)()
+        _lib.call("esr_bcg_status", _lib.ptr(self.ws), self.pack.ninst, self.nchunks, ctypes.byref(a), out,
+                  self._stream())
+        return list(out)
+
+    def reset(self, x0: Optional[torch.Tensor] = None):
+        """Start vector for the next solve: the packed x0 (default) or a
+        packed FP64 tensor of length n."""
+        src = torch.from_numpy(self.pack.x0).to(self.dev) if x0 is None else x0.to(self.dev, torch.float64)
+        self.x.copy_(split_df64(src) if self.precision == "df64" else src)
+
+    def load_instance(self, i: int, b: Optional[torch.Tensor] = None, x0: Optional[torch.Tensor] = None):
+        """Replace instance i's right hand side and/or start vector (FP64,
+        length = the instance's size) in the packed device vectors."""
+        rows = self.pack.rows(i)
+        conv = split_df64 if self.precision == "df64" else (lambda a: a)
+        if b is not None:
+            b = b.to(self.dev, torch.float64)
+            self.b64[rows] = b
+            self.b[rows] = conv(b)
+        if x0 is not None:
+            self.x[rows] = conv(x0.to(self.dev, torch.float64))
+
+    # ---------------------------------------------------------- autotune --
+    def autotune(self, tiles=(1, 2, 4, 8, 16), ctas_per_sm=(2, 3, 4, 6, 8), iters: int = 8, reps: int = 2) -> dict:
+        """Times ``iters`` lockstep iterations (every instance running) for
+        each (tiles per chunk, persistent CTAs per SM) pair on this batch and
+        keeps the fastest.  Leaves x untouched; the next ``run`` starts from
+        scratch.  Results are cached per batch signature in-process."""
+        key = (self.precision, self.pack.n, self.pack.ninst, int(self.pack.slice_ptr[-1]), self.jacobi)
+        hit = _TUNE_CACHE.get(key)
+        if hit is not None:
+            self.set_shape(hit["tiles_per_chunk"], hit["grid"])
+            self.tuning = dict(hit, cached=True)
+            return self.tuning
+        x_keep = self.x.clone()
+        stream = torch.cuda.current_stream(self.dev)
+        table = []
+        for m in tiles:
+            for c in ctas_per_sm:
+                self.set_shape(m, c * self.sm_count)
+                self.start(0.0, None, None)
+                self._iterate_call(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                best = float("inf")
+                for _ in range(reps):
+                    e0.record(stream)
+                    self._iterate_call(iters)
+                    e1.record(stream)
+                    e1.synchronize()
+                    best = min(best, e0.elapsed_time(e1) / iters)
+                table.append({"tiles_per_chunk": m, "ctas_per_sm": c, "ms_per_iter": best})
+        self.x.copy_(x_keep)
+        win = min(table, key=lambda r: r["ms_per_iter"])
+        res = {"tiles_per_chunk": win["tiles_per_chunk"], "grid": win["ctas_per_sm"] * self.sm_count,
+               "ms_per_iter": win["ms_per_iter"], "table": table}
+        _TUNE_CACHE[key] = res
+        self.set_shape(res["tiles_per_chunk"], res["grid"])
+        self.tuning = dict(res, cached=False)
+        return self.tuning
+
+    # ------------------------------------------------------------- solve --
+    def start(self, rtol: float, atol: Optional[float], maxiter: Optional[int]):
+        _lib.call("esr_bcg_init", ctypes.byref(self.desc), _lib.ptr(self.b64), _lib.ptr(self.b), _lib.ptr(self.x),
+                  _lib.ptr(self.r), _lib.ptr(self.z), _lib.ptr(self.p), float(rtol), float(atol) if atol else 0.0,
+                  -1 if maxiter is None else int(maxiter), _lib.ptr(self.ws), self._stream())
+        self.kernel_launches += 1
+
+    def verify(self):
+        _lib.call("esr_bcg_verify", ctypes.byref(self.desc), _lib.ptr(self.b64), _lib.ptr(self.x),
+                  _lib.ptr(self.x64), _lib.ptr(self.r64), _lib.ptr(self.r), _lib.ptr(self.z), _lib.ptr(self.p),
+                  _lib.ptr(self.ws), self._stream())
+        self.kernel_launches += 4
+
+    def run(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: Optional[int] = None,
+            max_rounds: int = 16) -> int:
+        """Device part of a solve; returns the number of verification rounds."""
+        self.start(rtol, atol, maxiter)
+        k = min(8, self.graph_iters)
+        rounds = 0
+        while True:
+            active = self.active()
+            while active > 0:
+                self._group(k)
+                k = min(self.graph_iters, 2 * k)
+                active = self.active()
+            self.verify()
+            rounds += 1
+            if self.active() == 0 or rounds >= max_rounds:
+                return rounds
+
+    def solve(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: Optional[int] = None,
+              max_rounds: int = 16) -> List[dict]:
+        """Solves every instance to ``||r|| <= max(rtol*||b||, atol)`` and
+        returns one dict per instance: status, iters (reference counting:
+        step() calls - 1), the final recurrence residual, the FP64 true
+        residual and the number of residual replacements."""
+        self.run(rtol, atol, maxiter, max_rounds)
+        return [self._info(s) for s in self.instances()]
+
+    @staticmethod
+    def _info(s) -> dict:
+        status = STATUS.get(s.done, "?")
+        if s.done == 1 and s.verified != 1:
+            status = "unverified"
+        tr = float(s.true_rr) ** 0.5 if s.true_rr >= 0 else float("nan")
+        return {"status": status, "iters": max(int(s.iters) - 1, 0), "residual": float(s.rr) ** 0.5,
+                "true_residual": tr, "bnorm": float(s.bnorm), "tol": float(s.tol), "restarts": int(s.restarts)}
+
+    def solution(self, i: Optional[int] = None) -> torch.Tensor:
+        """FP64 solution of instance i (all packed rows when None)."""
+        x = join_df64(self.x) if self.precision == "df64" else self.x
+        return x if i is None else x[self.pack.rows(i)]
+
+
+_TUNE_CACHE: dict = {}
+
+
+def p1_instances(count: int, nmin: int, nmax: int, seed: int = 0, corr_len: float = 0.1,
+                 variance: float = 1.0) -> List[LinsysInstance]:
+    """Seeded batch of P1 Poisson instances: side N ~ U{nmin..nmax},
+    kappa = exp(g) with g a Gaussian random field (correlation length
+    corr_len, variance), 16-mode random right hand side."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(nmin, nmax + 1, count)
+    out = []
+    for i, n in enumerate(sides):
+        n = int(n)
+        kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, seed * 100_003 + 2 * i, corr_len, variance))
+        s = mesh.p1_system(n, kappa)
+        b = mesh.random_mode_rhs(n, seed * 100_003 + 2 * i + 1)
+        out.append(LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, b))
+    return out

@@ -107,14 +107,19 @@ class CG(esr.Module):
         A = self.A
         key = (precision, A.Ae.data.data_ptr(), A.Ae._version, A.Av.data.data_ptr(), A.Av._version)
         if self._fused is None or self._fused_key != key:
-            sell = SellMatrix.from_linsys(A)
             jacobi = isinstance(self.M, Jacobi)
+            if precision in ("mixed", "df64") and A.Av.dtype != torch.float64:
+                raise ValueError(f"precision='{precision}' needs an FP64 system")
             if precision == "mixed":
-                if sell.dtype != torch.float64:
-                    raise ValueError("precision='mixed' needs an FP64 system")
-                self._fused = MixedPCG(sell, jacobi=jacobi)
+                self._fused = MixedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
+            elif precision == "df64":
+                from ..batched import BatchedPCG, LinsysInstance
+                n = A.Av.shape[0]
+                inst = LinsysInstance(n, A.reducer.idx.detach().cpu().numpy(), A.selector.idx.detach().cpu().numpy(),
+                                      A.Ae.data, A.Av.data, self.b.data)
+                self._fused = BatchedPCG([inst], jacobi=jacobi, precision="df64", device=self.x.device)
             else:
-                self._fused = FusedPCG(sell, jacobi=jacobi)
+                self._fused = FusedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
             self._fused_key = key
         return self._fused
 
@@ -126,7 +131,10 @@ class CG(esr.Module):
         ``precision='native'`` iterates in the system's dtype;
         ``'mixed'`` (FP64 systems) runs the SpMV on FP32 matrix values and an
         FP32 copy of p, keeps the vectors and dots in FP64, replaces the
-        residual by the FP64 true residual every 32 iterations and stops on it.
+        residual by the FP64 true residual every 32 iterations and stops on it;
+        ``'df64'`` (FP64 systems) iterates in double-float arithmetic (FP32
+        pairs, ~48 significand bits) and accepts the result only when the FP64
+        true residual meets the tolerance (restarting from it otherwise).
         Returns ``{'residual', 'iters'}`` as the reference, plus
         ``'true_residual'`` (||b - A x||, FP64) on the fused path.
         """
@@ -135,7 +143,7 @@ class CG(esr.Module):
         if use_fused and debug_iter is None:
             return self._solve_fused(rtol, atol, maxiter, precision)
         if precision != "native":
-            raise ValueError("precision='mixed' needs the fused path (Linsys operator, Jacobi or no preconditioner)")
+            raise ValueError(f"precision='{precision}' needs the fused path (Linsys operator, Jacobi or no preconditioner)")
         self.init()
         rtol_t = rtol * self.bnorm
         tol = torch.maximum(rtol_t, torch.as_tensor(atol, dtype=rtol_t.dtype, device=rtol_t.device)) \
@@ -157,7 +165,16 @@ class CG(esr.Module):
         name = self.__class__.__name__
         eng = self._fused_solver(precision)
         x, b = self.x.data, self.b.data
-        if precision == "mixed":
+        if precision == "df64":
+            eng.load_instance(0, b=b, x0=x)
+            [res] = eng.solve(rtol, atol, maxiter)
+            x.copy_(eng.solution(0).to(x.dtype))
+            rn = res["true_residual"]
+            self.rnorm.data.fill_(res["residual"])
+            self.bnorm.data.fill_(res["bnorm"])
+            info = {"residual": res["residual"], "iters": res["iters"], "true_residual": rn,
+                    "restarts": res["restarts"], "precision": "df64", "status": res["status"]}
+        elif precision == "mixed":
             s = eng.solve(b, x, self.r.data, self.z.data, self.p.data, rtol, atol, maxiter)
             rn = float(s.true_rr) ** 0.5
             self.rnorm.data.fill_(rn)

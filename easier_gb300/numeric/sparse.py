@@ -93,6 +93,13 @@ class FusedPCG:
         self._graphs = {}
         self.kernel_launches = 0
 
+    def bytes_per_iteration(self) -> int:
+        """Algorithmic HBM bytes of one iteration: the SpMV streams col, val,
+        slice_ptr and diag, gathers p and writes q; the update reads x, r, p,
+        q, invdiag and writes x, r, z; the p-update reads z, p and writes p."""
+        s = self.A.val.element_size()
+        return self.A.col.numel() * (4 + s) + self.A.slice_ptr.numel() * 8 + self.n * 14 * s
+
     def _iterate_call(self, x, r, z, p, k):
         _lib.call("esr_cg_iterate", ctypes.byref(self.A.desc), _lib.ptr(x), _lib.ptr(r), _lib.ptr(z), _lib.ptr(p),
                   _lib.ptr(self.q), _lib.ptr(self.invdiag), int(k), _lib.ptr(self.ws), _lib.stream_handle(self.dev))
@@ -168,6 +175,17 @@ class MixedPCG:
         self.use_graph = use_graph
         self._graphs = {}
         self.kernel_launches = 0
+
+    def bytes_per_iteration(self) -> int:
+        """FP32 SpMV (col, val32, p32 gather, diag32) plus FP64 vectors: the
+        update reads x, r, p, q, invdiag and writes x, r, z; the p-update
+        reads z, p and writes p and p32; the chunk's true residual is
+        amortised over ``chunk`` iterations."""
+        A, n = self.A32, self.n
+        spmv = A.col.numel() * 8 + A.slice_ptr.numel() * 8 + n * (4 + 4 + 8 + 8)
+        vec = n * 8 * 8 + n * (8 * 3 + 4)
+        tr = (self.A64.col.numel() * 12 + n * 8 * 4) / self.chunk
+        return int(spmv + vec + tr)
 
     def _iterate_call(self, b, x, r, z, p):
         _lib.call("esr_cg_mixed_iterate", ctypes.byref(self.A64.desc), ctypes.byref(self.A32.desc), _lib.ptr(b),

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 2
+#define ESR_GB300_ABI_VERSION 3
 
 /* element types */
 enum {
@@ -427,6 +427,90 @@ int esr_convert(int dtype_in, const void *in, int dtype_out, void *out,
  * correction of mixed-precision CG (no reference counterpart). */
 int esr_axpy_f64(double *x, int dtype_d, const void *d, double scale,
                  int64_t n, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Batched (P)CG: `ninst` independent Linsys instances packed as one
+ * block-diagonal SELL-32 system and iterated in lockstep, each with its own
+ * scalars and stopping test (easier/numeric/solver/cg.py:68-161 per
+ * instance).  A single system is a batch of one.  No reference counterpart
+ * for batching or df64: the reference runs one FP64 system per call.
+ *
+ * Layout: instance i owns the 256-row tiles [inst_block0[i],
+ * inst_block0[i+1]) (padded with identity rows: diag 1, b 0), and no column
+ * of an instance points into another.  Consecutive tiles of an instance are
+ * grouped into chunks (chunk c = tiles [chunk_tile0[c], chunk_tile0[c+1]),
+ * all of instance chunk_inst[c]; instance i owns chunks [inst_chunk0[i],
+ * inst_chunk0[i+1])).  The per-iteration kernels run `grid` persistent CTAs
+ * of 256 threads that loop over the chunks of the running instances.
+ *
+ * df64 = 0: val/diag/invdiag and the vectors x, r, z, p, q are FP64.
+ * df64 = 1: they are double-float pairs {float hi, lo} (8 bytes per value,
+ *           hi + lo), the arithmetic runs on the FP32 pipes with ~48
+ *           significand bits; val64/diag64 (FP64) serve the true-residual
+ *           check of esr_bcg_verify. */
+typedef struct {
+  int64_t n;               /* packed rows = 256 * nblocks                  */
+  int32_t ninst;
+  int32_t nblocks;         /* 256-row tiles                                */
+  int32_t rows_per_block;  /* must be 256                                  */
+  int32_t df64;
+  int32_t nchunks;
+  int32_t grid;            /* persistent CTAs of the iteration kernels     */
+  const int64_t *slice_ptr;  /* [n/32 + 1]                                 */
+  const int32_t *col;        /* [nslots], -1 = padding                     */
+  const void *val;           /* [nslots] FP64 or df64                      */
+  const void *diag;          /* [n]                                        */
+  const void *invdiag;       /* [n] Jacobi 1/diag, NULL = no preconditioner */
+  const double *val64;       /* [nslots] FP64 (verification)               */
+  const double *diag64;      /* [n]                                        */
+  const int32_t *block_inst; /* [nblocks] instance of each tile            */
+  const int32_t *inst_block0;/* [ninst + 1] first tile of each instance    */
+  const int32_t *chunk_tile0;/* [nchunks + 1] first tile of each chunk     */
+  const int32_t *chunk_inst; /* [nchunks] instance of each chunk           */
+  const int32_t *inst_chunk0;/* [ninst + 1] first chunk of each instance   */
+} esr_batch;
+
+/* Per-instance device scalars. */
+typedef struct {
+  double rz, pq, alpha, beta, rr, bnorm, tol;
+  double true_rr;    /* FP64 ||b - A x||^2 of the last verification, -1 none */
+  int32_t iters;     /* completed step() calls                              */
+  int32_t done;      /* 0 running, 1 converged, 2 maxiter, 3 breakdown/NaN  */
+  int32_t verified;  /* 1 = FP64 true residual <= tol                       */
+  int32_t restarts;  /* residual replacements after a failed verification   */
+  int32_t maxiter;
+  int32_t pad_;
+} esr_bcg_inst;
+
+int64_t esr_bcg_workspace_bytes(int32_t ninst, int32_t nblocks,
+                                int32_t nchunks);
+
+/* Per instance: r = b - A x, z = M r, p = z, bnorm = ||b64||,
+ * tol = max(rtol*bnorm, atol); counts every instance as running.  Zeroes
+ * the workspace. */
+int esr_bcg_init(const esr_batch *B, const double *b64, const void *b, void *x,
+                 void *r, void *z, void *p, double rtol, double atol,
+                 int32_t maxiter, void *workspace, void *stream);
+
+/* One compaction launch (lists the chunks of running instances) and `k`
+ * lockstep iterations of 3 persistent launches each.  Instances that stop
+ * inside the call skip their chunks; the host enqueues calls (e.g. as CUDA
+ * graphs) and polls esr_bcg_status between them.  q is scratch [n]. */
+int esr_bcg_iterate(const esr_batch *B, void *x, void *r, void *z, void *p,
+                    void *q, int32_t k, void *workspace, void *stream);
+
+/* For every converged, unverified instance: x64 = x, r64 = b64 - A64 x64 in
+ * FP64; verified = 1 when ||r64|| <= tol.  Otherwise r = r64 replaces the
+ * recurrence residual (z = M r, p = z + (r.z / r.z_old) p) and the
+ * instance runs again.  4 launches. */
+int esr_bcg_verify(const esr_batch *B, const double *b64, void *x, double *x64,
+                   double *r64, void *r, void *z, void *p, void *workspace,
+                   void *stream);
+
+/* Running-instance count and (if inst_out) the per-instance scalars, to
+ * host memory; synchronises `stream`. */
+int esr_bcg_status(const void *workspace, int32_t ninst, int32_t nchunks,
+                   int32_t *active, esr_bcg_inst *inst_out, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,103 @@
+"""Host packing of the batched PCG: the block-diagonal SELL-32 system applies
+each instance's Linsys exactly (checked against the oracle's
+index-multiply-scatter-add), padding rows are identity rows, no column
+crosses an instance, and the df64 split is exact to ~48 bits."""
+import numpy as np
+import torch
+
+from easier_gb300 import mesh
+from easier_gb300.numeric.batched import (ROWS_PER_BLOCK, LinsysInstance, PackedBatch, join_df64, p1_instances,
+                                          split_df64)
+from oracle import sparse as osp
+
+
+def _sell_apply(pk: PackedBatch, x: np.ndarray) -> np.ndarray:
+    y = pk.diag * x
+    nsl = pk.n // 32
+    for s in range(nsl):
+        b, e = int(pk.slice_ptr[s]), int(pk.slice_ptr[s + 1])
+        w = (e - b) // 32
+        for k in range(w):
+            sl = slice(b + 32 * k, b + 32 * k + 32)
+            c = pk.col[sl]
+            ok = c >= 0
+            rows = 32 * s + np.arange(32)
+            y[rows[ok]] += pk.val[sl][ok] * x[c[ok]]
+    return y
+
+
+def test_pack_applies_each_instance():
+    rng = np.random.default_rng(0)
+    insts = []
+    for n in (5, 9, 20):  # 16, 64 and 361 unknowns: one partial block, one, two
+        kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, n))
+        s = mesh.p1_system(n, kappa)
+        insts.append(LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, rng.standard_normal(s.nunk)))
+    pk = PackedBatch(insts)
+    assert pk.n == ROWS_PER_BLOCK * pk.nblocks
+    assert list(pk.inst_block0) == [0, 1, 2, 4]
+    assert list(pk.block_inst) == [0, 1, 2, 2]
+    x = rng.standard_normal(pk.n)
+    y = _sell_apply(pk, x)
+    for i, s in enumerate(insts):
+        rows = pk.rows(i)
+        ref = osp.linsys_apply(torch.from_numpy(x[rows].copy()), s.row, s.col, torch.from_numpy(s.Ae),
+                               torch.from_numpy(s.Av)).numpy()
+        assert np.allclose(y[rows], ref, rtol=1e-13, atol=1e-13)
+        assert np.array_equal(pk.b[rows], s.b)
+        # columns of instance i stay inside its padded block range
+        lo, hi = int(pk.row0[i]), int(pk.inst_block0[i + 1]) * ROWS_PER_BLOCK
+        s0 = lo // 32
+        s1 = hi // 32
+        c = pk.col[pk.slice_ptr[s0]:pk.slice_ptr[s1]]
+        c = c[c >= 0]
+        assert c.size and c.min() >= lo and c.max() < lo + s.n
+    pad = np.ones(pk.n, bool)
+    for i in range(len(insts)):
+        pad[pk.rows(i)] = False
+    assert np.all(pk.diag[pad] == 1.0) and np.all(pk.b[pad] == 0.0)
+    assert np.array_equal(y[pad], x[pad])
+
+
+def test_pack_empty_and_exact_block_instances():
+    s = mesh.p1_system(17)  # 256 unknowns: exactly one block, no padding
+    pk = PackedBatch([LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, np.ones(s.nunk)),
+                      LinsysInstance(0, np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0), np.zeros(0),
+                                     np.zeros(0))])
+    assert s.nunk == 256 and pk.nblocks == 2 and list(pk.inst_block0) == [0, 1, 2]
+
+
+def test_df64_split_roundtrip():
+    rng = np.random.default_rng(3)
+    v = torch.from_numpy(rng.standard_normal(1000) * 10.0 ** rng.integers(-8, 8, 1000))
+    d = split_df64(v)
+    assert d.dtype == torch.float32 and d.shape == (1000, 2)
+    err = (join_df64(d) - v).abs() / v.abs()
+    assert float(err.max()) < 2.0 ** -47
+    # hi is the FP32 rounding of v, and |lo| <= ulp(hi) / 2
+    assert torch.equal(d[:, 0], v.to(torch.float32))
+
+
+def test_p1_instances_seeded():
+    a = p1_instances(3, 8, 16, seed=5)
+    b = p1_instances(3, 8, 16, seed=5)
+    assert [s.n for s in a] == [s.n for s in b]
+    for s, t in zip(a, b):
+        assert np.array_equal(s.Ae, t.Ae) and np.array_equal(s.b, t.b)
+        m = int(round(np.sqrt(s.n))) + 1
+        assert 8 <= m <= 16 and (m - 1) ** 2 == s.n
+
+
+def test_chunk_layout():
+    from easier_gb300.numeric.batched import chunk_layout
+    ib0 = np.array([0, 1, 2, 4, 14], np.int32)
+    ct0, ci, ic0 = chunk_layout(ib0, 4)
+    assert list(ct0) == [0, 1, 2, 4, 8, 12, 14]
+    assert list(ci) == [0, 1, 2, 3, 3, 3]
+    assert list(ic0) == [0, 1, 2, 3, 6]
+    for m in (1, 3, 16):
+        ct0, ci, ic0 = chunk_layout(ib0, m)
+        assert ct0[0] == 0 and ct0[-1] == 14 and np.all(np.diff(ct0) >= 1) and np.all(np.diff(ct0) <= m)
+        # every chunk lies inside its instance's tiles
+        assert np.all(ct0[:-1] >= ib0[ci]) and np.all(ct0[1:] <= ib0[ci + 1])
+        assert np.array_equal(np.searchsorted(ic0, np.arange(len(ci)), side="right") - 1, ci)
