@@ -364,6 +364,7 @@ def bench_poisson(args, world, rank, local):
         "config": {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to FP64 true rel. residual 1e-8",
                    "unknowns": eqn.nunk, "couplings": int(eqn.selector.idx.numel()), "iterations": nit,
                    "precision": args.precision, "bytes_per_iteration": bytes_it,
+                   "replacements": info.get("restarts", info.get("replacements")),
                    "true_rel_residual": rel, "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None},

@@ -17,7 +17,7 @@ from .utils import EasierJitException
 F32, F64, I32, I64 = 0, 1, 2, 3
 REDUCE_OPS = {"sum": 0, "prod": 1, "mean": 2, "amax": 3, "amin": 4}
 AGG_SUM, AGG_PROD, AGG_NORM, AGG_MAX, AGG_MIN = 0, 1, 2, 3, 4
-DEV_IDX_RANGE, DEV_NONFINITE = 1, 2
+DEV_IDX_RANGE, DEV_NONFINITE, DEV_WAIT_TIMEOUT = 1, 2, 4
 
 _LOCK = threading.Lock()
 _LIB = None
@@ -50,19 +50,29 @@ class CgScalars(Structure):
                 ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("replacements", c_int32)]
 
 
+class Gnn(Structure):
+    _fields_ = [("node_lk", c_void_p), ("edge_feat", c_void_p), ("inst_rows", c_void_p), ("h0", c_void_p),
+                ("h1", c_void_p), ("enc_w", c_void_p), ("enc_b", c_void_p), ("layer_w", c_void_p),
+                ("layer_b", c_void_p), ("dec_w", c_void_p), ("dec_b", ctypes.c_float), ("grid", c_int32),
+                ("stall_window", c_int32), ("pad_", c_int32)]
+
+
 class Batch(Structure):
     _fields_ = [("n", c_int64), ("ninst", c_int32), ("nblocks", c_int32), ("rows_per_block", c_int32),
                 ("df64", c_int32), ("nchunks", c_int32), ("grid", c_int32), ("slice_ptr", c_void_p),
                 ("col", c_void_p), ("val", c_void_p), ("diag", c_void_p), ("invdiag", c_void_p),
                 ("val64", c_void_p), ("diag64", c_void_p), ("block_inst", c_void_p), ("inst_block0", c_void_p),
-                ("chunk_tile0", c_void_p), ("chunk_inst", c_void_p), ("inst_chunk0", c_void_p)]
+                ("chunk_tile0", c_void_p), ("chunk_inst", c_void_p), ("inst_chunk0", c_void_p),
+                ("gnn", POINTER(Gnn))]
 
 
 class BcgInst(Structure):
     _fields_ = [("rz", c_double), ("pq", c_double), ("alpha", c_double), ("beta", c_double),
                 ("rr", c_double), ("bnorm", c_double), ("tol", c_double), ("true_rr", c_double),
+                ("sigma", c_double), ("rr_mark", c_double), ("rz_jac", c_double),
                 ("iters", c_int32), ("done", c_int32), ("verified", c_int32), ("restarts", c_int32),
-                ("maxiter", c_int32), ("pad_", c_int32)]
+                ("maxiter", c_int32), ("mode", c_int32), ("refresh", c_int32), ("fallbacks", c_int32),
+                ("nrows", c_int32), ("pad_", c_int32)]
 
 
 _P = c_void_p
@@ -111,9 +121,10 @@ _SIGS = {
     "esr_bcg_iterate": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, c_int32, _P, _P]),
     "esr_bcg_verify": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "esr_bcg_status": (c_int, [_P, c_int32, c_int32, POINTER(c_int32), POINTER(BcgInst), _P]),
+    "esr_gnn_apply": (c_int, [POINTER(Batch), _P, _P, _P, _P]),
 }
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 
 def library_path() -> Path:

@@ -5,6 +5,9 @@
 // Iteration per instance (easier/numeric/solver/cg.py:68-95, Jacobi M):
 //   q = A p; alpha = r.z / p.q; x += alpha p; r -= alpha q; z = M r;
 //   stop when ||r|| <= tol; beta = r.z_new / r.z; p = z + beta p
+// With the GNN preconditioner (esr_batch.gnn, gnn.cu) the iteration is
+// flexible CG: z = M(r) is the network's output and beta takes the
+// Polak-Ribiere form z.(r - r_old) / z_old.r_old = -alpha z.q / z_old.r_old.
 //
 // Work decomposition.  Every instance is padded to whole 256-row tiles
 // (identity rows), so no tile spans two instances.  Consecutive tiles of an
@@ -29,222 +32,9 @@
 // residual misses the tolerance continues from it: r = b - A x replaces the
 // recurrence residual and p keeps its direction (a residual replacement,
 // not a restart).
-#include <cmath>
-#include <cstdint>
-
-#include "df64.cuh"
-#include "esr_internal.h"
-#include "reduce_util.cuh"
+#include "bcg_common.cuh"
 
 namespace {
-
-constexpr int kBThreads = 256;  // rows per tile: one row per thread per tile
-constexpr int kBSums = 3;       // partial arrays
-
-struct BcgHead {
-  int32_t active;  // instances with done == 0
-  int32_t acount;  // entries of the active chunk list
-  int32_t pad[62];
-};
-
-struct BcgLayout {
-  BcgHead *head;
-  esr_bcg_inst *inst;
-  unsigned int *counter;  // [ninst] arrival tickets
-  int32_t *alist;         // [nchunks] active chunk list
-  double *partial;        // [kBSums][nblocks] (chunk or tile partials)
-};
-
-inline int64_t round256(int64_t v) { return (v + 255) / 256 * 256; }
-
-BcgLayout layout_of(void *ws, int32_t ninst, int32_t nchunks) {
-  char *p = (char *)ws;
-  BcgLayout L;
-  L.head = (BcgHead *)p;
-  p += round256(sizeof(BcgHead));
-  L.inst = (esr_bcg_inst *)p;
-  p += round256(ninst * (int64_t)sizeof(esr_bcg_inst));
-  L.counter = (unsigned int *)p;
-  p += round256(ninst * (int64_t)sizeof(unsigned int));
-  L.alist = (int32_t *)p;
-  p += round256(nchunks * (int64_t)sizeof(int32_t));
-  L.partial = (double *)p;
-  return L;
-}
-
-int64_t workspace_bytes(int32_t ninst, int32_t nblocks, int32_t nchunks) {
-  return round256(sizeof(BcgHead)) + round256(ninst * (int64_t)sizeof(esr_bcg_inst)) +
-         round256(ninst * (int64_t)sizeof(unsigned int)) + round256(nchunks * (int64_t)sizeof(int32_t)) +
-         kBSums * (int64_t)nblocks * (int64_t)sizeof(double);
-}
-
-// ---- arithmetic policies
-struct DotAccD {
-  double v = 0.0;
-  __device__ __forceinline__ void add(double a, double b) { v = fma(a, b, v); }
-  __device__ __forceinline__ double value() const { return v; }
-};
-
-struct DotAccDF {  // hi*hi products exactly (two-prod + two-sum), cross terms in lo
-  float hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add(df64::df a, df64::df b) {
-    const df64::df p = df64::two_prod(a.hi, b.hi);
-    const df64::df s = df64::two_sum(hi, p.hi);
-    hi = s.hi;
-    lo = __fadd_rn(lo, __fadd_rn(s.lo, __fadd_rn(p.lo, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi)))));
-  }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
-struct PolF64 {
-  using V = double;
-  using Acc = DotAccD;
-  static __device__ __forceinline__ V fma(V a, V b, V c) { return ::fma(a, b, c); }
-  static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
-  static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
-  static __device__ __forceinline__ V of(double d) { return d; }
-  static __device__ __forceinline__ V zero() { return 0.0; }
-  static __device__ __forceinline__ double dbl(V a) { return a; }
-};
-
-struct PolDF {
-  using V = df64::df;
-  using Acc = DotAccDF;
-  static __device__ __forceinline__ V fma(V a, V b, V c) { return df64::fma(a, b, c); }
-  static __device__ __forceinline__ V mul(V a, V b) { return df64::mul(a, b); }
-  static __device__ __forceinline__ V sub(V a, V b) { return df64::add(a, df64::neg(b)); }
-  static __device__ __forceinline__ V of(double d) { return df64::from_double(d); }
-  static __device__ __forceinline__ V zero() { return V{0.f, 0.f}; }
-  static __device__ __forceinline__ double dbl(V a) { return df64::to_double(a); }
-};
-
-// sum over the row's SELL slots of val * x, in slot order
-template <class P>
-__device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
-                                                   const int32_t *__restrict__ col,
-                                                   const typename P::V *__restrict__ val,
-                                                   const typename P::V *__restrict__ x) {
-  using V = typename P::V;
-  const int64_t s = i >> 5;
-  const int lane = (int)(i & 31);
-  const int64_t b = __ldg(slice_ptr + s);
-  const int w = (int)((__ldg(slice_ptr + s + 1) - b) >> 5);
-  const int32_t *cp = col + b + lane;
-  const V *vp = val + b + lane;
-  V acc = P::zero();
-  if (w <= 8) {
-    int32_t c[8];
-    V v[8], xc[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      c[k] = k < w ? __ldg(cp + 32 * k) : -1;
-      if ((int64_t)c[k] >= n) c[k] = -1;
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (c[k] >= 0) {
-        v[k] = vp[32 * k];
-        xc[k] = x[c[k]];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (c[k] >= 0) acc = P::fma(v[k], xc[k], acc);
-    return acc;
-  }
-  for (int k = 0; k < w; ++k) {
-    const int32_t c = __ldg(cp + 32 * k);
-    if (c >= 0 && (int64_t)c < n) acc = P::fma(vp[32 * k], x[c], acc);
-  }
-  return acc;
-}
-
-// FP64 row of the true residual
-__device__ __forceinline__ double bsell_row64(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
-                                              const int32_t *__restrict__ col, const double *__restrict__ val,
-                                              const double *__restrict__ x) {
-  const int64_t s = i >> 5;
-  const int lane = (int)(i & 31);
-  const int64_t b = __ldg(slice_ptr + s);
-  const int w = (int)((__ldg(slice_ptr + s + 1) - b) >> 5);
-  double acc = 0.0;
-  for (int k = 0; k < w; ++k) {
-    const int64_t e = b + 32 * k + lane;
-    const int32_t c = __ldg(col + e);
-    if (c >= 0 && (int64_t)c < n) acc = fma(__ldg(val + e), __ldg(x + c), acc);
-  }
-  return acc;
-}
-
-// Per-instance finish of K sums.  The calling CTA publishes its K block
-// sums at partial[k][slot] and takes an arrival ticket on the instance's
-// counter; the CTA holding the last of `expected` tickets (returns true in
-// all its threads) adds partial[k][p0..p1) in order into tot and resets the
-// counter.  Never waits on another CTA.
-template <int K>
-__device__ __forceinline__ bool inst_finish(const double (&v)[K], int slot, int p0, int p1, int expected,
-                                            int nblocks, double *partial, unsigned int *counter, double (&tot)[K]) {
-  __shared__ double s_red[kBThreads / 32];
-  __shared__ bool s_last;
-  double bs[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) bs[k] = esr::block_sum_fixed<kBThreads>(v[k], s_red);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) partial[k * (int64_t)nblocks + slot] = bs[k];
-    __threadfence();
-    const unsigned int t = atomicAdd(counter, 1u);
-    s_last = (t == (unsigned int)(expected - 1));
-  }
-  __syncthreads();
-  if (!s_last) return false;
-  __threadfence();
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double acc = 0.0;
-    for (int q = p0 + threadIdx.x; q < p1; q += kBThreads) acc += __ldcg(partial + k * (int64_t)nblocks + q);
-    tot[k] = esr::block_sum_fixed<kBThreads>(acc, s_red);
-  }
-  if (threadIdx.x == 0) *counter = 0u;
-  return true;
-}
-
-struct BArgs {
-  int64_t n;
-  int32_t nblocks;
-  int32_t ninst;
-  int32_t nchunks;
-  const int64_t *slice_ptr;
-  const int32_t *col;
-  const int32_t *block_inst;
-  const int32_t *inst_block0;
-  const int32_t *chunk_tile0;
-  const int32_t *chunk_inst;
-  const int32_t *inst_chunk0;
-};
-
-inline BArgs bargs(const esr_batch *B) {
-  return BArgs{B->n,         B->nblocks,     B->ninst,       B->nchunks,     B->slice_ptr, B->col,
-               B->block_inst, B->inst_block0, B->chunk_tile0, B->chunk_inst, B->inst_chunk0};
-}
-
-__device__ __forceinline__ void retire(BcgLayout L) { atomicSub(&L.head->active, 1); }
-
-// tile-grid finish (init / verify kernels: one CTA per tile)
-template <int K>
-__device__ __forceinline__ bool tile_finish(const BArgs &a, int inst, const double (&v)[K], BcgLayout L,
-                                            double (&tot)[K]) {
-  const int b0 = a.inst_block0[inst], b1 = a.inst_block0[inst + 1];
-  return inst_finish<K>(v, blockIdx.x, b0, b1, b1 - b0, a.nblocks, L.partial, L.counter + inst, tot);
-}
-
-// chunk finish (persistent kernels)
-template <int K>
-__device__ __forceinline__ bool chunk_finish(const BArgs &a, int chunk, int inst, const double (&v)[K],
-                                             BcgLayout L, double (&tot)[K]) {
-  const int c0 = a.inst_chunk0[inst], c1 = a.inst_chunk0[inst + 1];
-  return inst_finish<K>(v, chunk, c0, c1, c1 - c0, a.nblocks, L.partial, L.counter + inst, tot);
-}
 
 // ---- compaction: list the chunks of running instances (one CTA)
 __global__ void __launch_bounds__(1024) bcg_compact_kernel(BArgs a, BcgLayout L) {
@@ -314,6 +104,13 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     s.verified = 0;
     s.restarts = 0;
     s.maxiter = maxiter;
+    s.mode = a.use_gnn ? kModeGnn : kModeJacobi;
+    s.refresh = 0;
+    s.fallbacks = 0;
+    s.nrows = a.use_gnn ? a.inst_rows[inst] : 0;
+    s.sigma = s.nrows > 0 ? sqrt(tot[2] / s.nrows) : 0.0;
+    s.rr_mark = tot[2];
+    s.rz_jac = tot[1];
     s.done = 0;  // the reference always takes a first step (cg.py:143-153)
     atomicAdd(&L.head->active, 1);
   }
@@ -367,6 +164,7 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
     const int inst = a.chunk_inst[c];
     if (L.inst[inst].done) continue;
     const double ad = L.inst[inst].alpha;
+    const bool gnn = L.inst[inst].mode == kModeGnn;  // z comes from the GNN layers
     const V av = P::of(ad), nav = P::of(-ad);
     typename P::Acc rr, rz;
     const int t1 = a.chunk_tile0[c + 1];
@@ -376,7 +174,7 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
       const V ri = P::fma(nav, q[i], r[i]);
       r[i] = ri;
       const V zi = invdiag ? P::mul(ri, invdiag[i]) : ri;
-      z[i] = zi;
+      if (!gnn) z[i] = zi;
       rr.add(ri, ri);
       rz.add(ri, zi);
     }
@@ -386,6 +184,8 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
       esr_bcg_inst &s = L.inst[inst];
       s.iters += 1;
       s.rr = tot[0];
+      s.rz_jac = tot[1];
+      s.refresh = 0;
       const double rnorm = sqrt(tot[0]);
       if (!isnan(rnorm) && rnorm <= s.tol) {
         s.done = 1;
@@ -396,6 +196,21 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
       } else if (!isfinite(rnorm) || !isfinite(tot[1]) || s.rz == 0.0) {
         s.done = 3;
         retire(L);
+      } else if (s.mode == kModeGnn) {
+        // beta follows from the GNN output (gnn.cu); here: input scale and
+        // the stall test (no decrease of r.r over a window -> Jacobi)
+        s.sigma = s.nrows > 0 ? sqrt(tot[0] / s.nrows) : 0.0;
+        if (a.stall_window > 0 && s.iters % a.stall_window == 0) {
+          if (!(tot[0] < s.rr_mark)) {
+            s.mode = kModeJacobi;
+            s.refresh = 1;
+            s.fallbacks += 1;
+            s.beta = 0.0;
+            s.rz = tot[1];
+          } else {
+            s.rr_mark = tot[0];
+          }
+        }
       } else {
         s.beta = tot[1] / s.rz;
         s.rz = tot[1];
@@ -405,9 +220,11 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
 }
 
 // ---- update part 2: p = z + beta p
+// (refresh: the instance just fell back to Jacobi: p = invdiag r)
 template <class P>
 __global__ void __launch_bounds__(kBThreads)
-bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V *__restrict__ p, BcgLayout L) {
+bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, const typename P::V *__restrict__ r,
+                   const typename P::V *__restrict__ invdiag, typename P::V *__restrict__ p, BcgLayout L) {
   using V = typename P::V;
   const int count = L.head->acount;
   for (int w = blockIdx.x; w < count; w += gridDim.x) {
@@ -415,10 +232,14 @@ bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V *
     const int inst = a.chunk_inst[c];
     if (L.inst[inst].done) continue;
     const V beta = P::of(L.inst[inst].beta);
+    const bool refresh = L.inst[inst].refresh != 0;
     const int t1 = a.chunk_tile0[c + 1];
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
       const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
-      p[i] = P::fma(beta, p[i], z[i]);
+      if (refresh)
+        p[i] = invdiag ? P::mul(r[i], invdiag[i]) : r[i];
+      else
+        p[i] = P::fma(beta, p[i], z[i]);
     }
   }
 }
@@ -481,8 +302,10 @@ bcg_replace_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const dou
   const double v[1] = {rz.value()};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
-    st.beta = (st.rz != 0.0) ? tot[0] / st.rz : 0.0;
+    // GNN mode: p restarts from the Jacobi direction (beta = 0)
+    st.beta = (st.mode != kModeGnn && st.rz != 0.0) ? tot[0] / st.rz : 0.0;
     st.rz = tot[0];
+    st.rz_jac = tot[0];
     st.rr = st.true_rr;
     st.verified = -2;  // p update pending
   }
@@ -508,17 +331,27 @@ bcg_replace_p_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V
   }
 }
 
-int check_batch(const esr_batch *B) {
-  if (!B) return esr::fail(ESR_ERR_ARG, "null batch");
-  if (B->n <= 0 || B->ninst <= 0 || B->nblocks <= 0 || B->nchunks <= 0) return esr::fail(ESR_ERR_ARG, "empty batch");
-  if (B->rows_per_block != kBThreads) return esr::fail(ESR_ERR_ARG, "rows_per_block must be 256");
-  if (B->n != (int64_t)B->nblocks * kBThreads) return esr::fail(ESR_ERR_ARG, "n must be nblocks * 256");
-  if (B->nchunks > B->nblocks || B->nchunks < B->ninst) return esr::fail(ESR_ERR_ARG, "bad chunk count");
-  if (B->grid <= 0) return esr::fail(ESR_ERR_ARG, "grid must be positive");
-  if (!B->slice_ptr || !B->col || !B->val || !B->diag || !B->val64 || !B->diag64 || !B->block_inst ||
-      !B->inst_block0 || !B->chunk_tile0 || !B->chunk_inst || !B->inst_chunk0)
-    return esr::fail(ESR_ERR_ARG, "null batch array");
-  return ESR_OK;
+// ---- standalone preconditioner application: every instance in GNN mode
+// with sigma = rms of r
+template <class P>
+__global__ void __launch_bounds__(kBThreads)
+gnn_prep_kernel(BArgs a, const typename P::V *__restrict__ r, BcgLayout L) {
+  const int inst = a.block_inst[blockIdx.x];
+  const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+  typename P::Acc rr;
+  if (i < a.n) rr.add(r[i], r[i]);
+  const double v[1] = {rr.value()};
+  double tot[1];
+  if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
+    esr_bcg_inst &s = L.inst[inst];
+    s.nrows = a.inst_rows[inst];
+    s.sigma = s.nrows > 0 ? sqrt(tot[0] / s.nrows) : 0.0;
+    s.rr = tot[0];
+    s.rz = 1.0;
+    s.alpha = 0.0;
+    s.mode = kModeGnn;
+    s.done = 0;
+  }
 }
 
 template <class P>
@@ -548,7 +381,12 @@ int run_iterate(const esr_batch *B, void *x, void *r, void *z, void *p, void *q,
                                                      (V *)q, L);
     bcg_update_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->invdiag, (V *)x, (V *)r, (V *)z,
                                                        (const V *)p, (const V *)q, L);
-    bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
+    if (B->gnn) {
+      const int st = esr::gnn_layers(B, r, q, z, ws, s);
+      if (st) return st;
+    }
+    bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (const V *)r, (const V *)B->invdiag,
+                                                        (V *)p, L);
   }
   ESR_LAUNCH_CHECK("esr_bcg_iterate");
   return ESR_OK;
@@ -568,7 +406,28 @@ int run_verify(const esr_batch *B, const double *b64, void *x, double *x64, doub
   return ESR_OK;
 }
 
+template <class P>
+int run_gnn_apply(const esr_batch *B, const void *r, void *z, void *ws, cudaStream_t s) {
+  BcgLayout L = layout_of(ws, B->ninst, B->nchunks);
+  const BArgs a = bargs(B);
+  cudaError_t e = cudaMemsetAsync(ws, 0, workspace_bytes(B->ninst, B->nblocks, B->nchunks), s);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_gnn_apply/memset");
+  gnn_prep_kernel<P><<<B->nblocks, kBThreads, 0, s>>>(a, (const typename P::V *)r, L);
+  bcg_compact_kernel<<<1, 1024, 0, s>>>(a, L);
+  ESR_LAUNCH_CHECK("esr_gnn_apply");
+  return esr::gnn_layers(B, r, r, z, ws, s);
+}
+
 }  // namespace
+
+extern "C" int esr_gnn_apply(const esr_batch *B, const void *r, void *z, void *workspace, void *stream) {
+  int st = check_batch(B);
+  if (st) return st;
+  if (!B->gnn) return esr::fail(ESR_ERR_ARG, "esr_gnn_apply needs batch.gnn");
+  if (!r || !z || !workspace) return esr::fail(ESR_ERR_ARG, "null vector");
+  cudaStream_t s = esr::as_stream(stream);
+  return B->df64 ? run_gnn_apply<PolDF>(B, r, z, workspace, s) : run_gnn_apply<PolF64>(B, r, z, workspace, s);
+}
 
 extern "C" int64_t esr_bcg_workspace_bytes(int32_t ninst, int32_t nblocks, int32_t nchunks) {
   if (ninst <= 0 || nblocks <= 0 || nchunks <= 0) return -1;

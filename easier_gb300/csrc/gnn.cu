@@ -1,0 +1,379 @@
+// GNN preconditioner of the batched flexible CG (bcg.cu): four message-
+// passing layers, hidden width 32, BF16 features, MLPs on the 5th-generation
+// tensor cores (tcgen05.mma, FP32 accumulator in tensor memory).
+//
+// One launch per layer.  Each is persistent over the active chunk list of
+// the batch and walks a chunk in 128-node tiles:
+//   1. aggregation (CUDA cores, FP32): 4 threads per node, 8 channels each,
+//      gather the neighbours' BF16 features over the node's SELL slots and
+//      form u = [h_i, sum_j w_ij h_j, sum_j len_ij h_j] (96 BF16) in shared
+//      memory, in the K-major core-matrix layout of the MMA (8 rows x 16 B
+//      core matrices; 128 B between core matrices along K, 1536 B between
+//      8-row groups);
+//   2. one thread issues 6 tcgen05.mma (M=128, N=32, K=16 each, BF16 in,
+//      FP32 accumulate) against the layer's weights, staged once per CTA in
+//      the same layout, and commits to an mbarrier;
+//   3. every warp reads its 32 accumulator lanes (tcgen05.ld 32x32b.x32),
+//      adds bias, ReLU and the residual h_i and stores BF16 h (layers 1-3),
+//      or (layer 4) decodes y_i = dec_w . h_i + dec_b and writes
+//      z_i = invdiag_i (r_i + sigma y_i), accumulating z.r and z.q for the
+//      instance's Polak-Ribiere beta.
+// Layer 1 evaluates the encoder h0 = relu(enc_w [r/sigma, lk] + enc_b) on
+// the fly for the node and its neighbours instead of storing h0.
+//
+// The mbarrier wait is bounded: on time-out the kernel raises
+// ESR_DEV_WAIT_TIMEOUT, stops, frees its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include "bcg_common.cuh"
+
+namespace {
+
+constexpr int kGThreads = 128;                    // CTA threads
+constexpr int kGRows = 128;                       // nodes per MMA tile (M)
+constexpr int kHid = 32;                          // hidden width (N)
+constexpr int kIn = 96;                           // MLP input (K) = [h, A, L]
+constexpr int kKChunks = kIn / 8;                 // 16-byte columns along K
+constexpr int kCoreBytes = 128;                   // one 8 x 16 B core matrix
+constexpr int kSBO = kKChunks * kCoreBytes;       // bytes between 8-row groups
+constexpr uint32_t kTmemCols = 32;                // FP32 accumulator columns
+constexpr int kWaitLimit = 1 << 22;               // mbarrier polls before giving up
+
+static_assert(kGThreads == kGRows, "one accumulator row per thread");
+static_assert(kBThreads % kGRows == 0, "tiles split into whole MMA tiles");
+
+// instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16 (bits 7-9
+// = 1), B BF16 (bits 10-12 = 1), A and B K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) |
+                            ((uint32_t)(kGRows >> 4) << 24);
+
+struct GArgs {
+  const float *node_lk;
+  const float2 *edge_feat;
+  const float *enc_w;
+  const float *enc_b;
+  const uint16_t *layer_w;
+  const float *layer_b;
+  const float *dec_w;
+  float dec_b;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, LBO = 128 B (next core
+// matrix along K), SBO = 1536 B (next 8-row group), version 1 (bits 46-47),
+// base offset 0, no swizzle
+__device__ __forceinline__ uint64_t mma_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(kCoreBytes >> 4) << 16) |
+         ((uint64_t)(kSBO >> 4) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint64_t *mbar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+  uint4 u;
+  __nv_bfloat162 t;
+  t = __floats2bfloat162_rn(f[0], f[1]);
+  u.x = *reinterpret_cast<uint32_t *>(&t);
+  t = __floats2bfloat162_rn(f[2], f[3]);
+  u.y = *reinterpret_cast<uint32_t *>(&t);
+  t = __floats2bfloat162_rn(f[4], f[5]);
+  u.z = *reinterpret_cast<uint32_t *>(&t);
+  t = __floats2bfloat162_rn(f[6], f[7]);
+  u.w = *reinterpret_cast<uint32_t *>(&t);
+  return u;
+}
+
+__device__ __forceinline__ void unpack8(uint4 u, float (&f)[8]) {
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    f[2 * k] = __uint_as_float(w[k] << 16);
+    f[2 * k + 1] = __uint_as_float(w[k] & 0xFFFF0000u);
+  }
+}
+
+__device__ __forceinline__ int sU_off(int m, int chunk) { return (m >> 3) * kSBO + chunk * kCoreBytes + (m & 7) * 16; }
+
+template <int LAYER, class P>
+__global__ void __launch_bounds__(kGThreads)
+gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const typename P::V *__restrict__ q,
+                 const typename P::V *__restrict__ invdiag, typename P::V *__restrict__ z,
+                 const uint4 *__restrict__ h_in, uint4 *__restrict__ h_out, BcgLayout L) {
+  using V = typename P::V;
+  __shared__ __align__(1024) uint8_t sU[kGRows * kIn * 2];
+  __shared__ __align__(1024) uint8_t sW[kHid * kIn * 2];
+  __shared__ float sBias[kHid];
+  __shared__ float sDec[kHid];
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_err;
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int part = tid & 3;  // aggregation: channels 8*part .. 8*part+7
+  {
+    const uint16_t *W = g.layer_w + (LAYER - 1) * kHid * kIn;
+    for (int e = tid; e < kHid * kKChunks; e += kGThreads) {
+      const int n = e / kKChunks, c = e % kKChunks;
+      *reinterpret_cast<uint4 *>(sW + sU_off(n, c)) = *reinterpret_cast<const uint4 *>(W + n * kIn + c * 8);
+    }
+    if (tid < kHid) {
+      sBias[tid] = g.layer_b[(LAYER - 1) * kHid + tid];
+      sDec[tid] = g.dec_w[tid];
+    }
+  }
+  if (tid == 0) {
+    mbar_init(&s_mbar);
+    s_err = 0;
+  }
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, kTmemCols);
+    tmem_relinquish();
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t tmem_warp = tmem + ((uint32_t)(warp * 32) << 16);
+
+  float ew0[8], ew1[8], eb[8];  // encoder rows of this thread's channels
+  if (LAYER == 1) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      ew0[k] = g.enc_w[(8 * part + k) * 2];
+      ew1[k] = g.enc_w[(8 * part + k) * 2 + 1];
+      eb[k] = g.enc_b[8 * part + k];
+    }
+  }
+
+  uint32_t phase = 0;
+  const int count = L.head->acount;
+  for (int w = blockIdx.x; w < count; w += gridDim.x) {
+    const int c = L.alist[w];
+    const int inst = a.chunk_inst[c];
+    const esr_bcg_inst &st = L.inst[inst];
+    if (st.done || st.mode != kModeGnn) continue;
+    const float sigma = (float)st.sigma;
+    const float inv_sigma = sigma > 0.f ? 1.f / sigma : 0.f;
+    const int64_t real_end = (int64_t)a.inst_block0[inst] * kBThreads + st.nrows;
+    typename P::Acc zr, zq;
+    const int64_t row1 = (int64_t)a.chunk_tile0[c + 1] * kBThreads;
+    bool stop = false;
+    for (int64_t s0 = (int64_t)a.chunk_tile0[c] * kBThreads; s0 < row1; s0 += kGRows) {
+      // ---- 1. aggregation into sU
+#pragma unroll 1
+      for (int pass = 0; pass < kGRows / 32; ++pass) {
+        const int m = pass * 32 + (tid >> 2);
+        const int64_t i = s0 + m;
+        float hs[8], accA[8], accL[8];
+        if (LAYER == 1) {
+          const float rh = P::flt(r[i]) * inv_sigma, lk = g.node_lk[i];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) hs[k] = bf16r(fmaxf(fmaf(ew0[k], rh, fmaf(ew1[k], lk, eb[k])), 0.f));
+        } else {
+          unpack8(h_in[i * 4 + part], hs);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) accA[k] = accL[k] = 0.f;
+        const int64_t sl = i >> 5;
+        const int ln = (int)(i & 31);
+        const int64_t base = a.slice_ptr[sl];
+        const int wd = (int)((a.slice_ptr[sl + 1] - base) >> 5);
+        for (int k = 0; k < wd; ++k) {
+          const int64_t e = base + 32 * k + ln;
+          const int32_t j = a.col[e];
+          if (j < 0 || (int64_t)j >= a.n) continue;
+          const float2 ef = g.edge_feat[e];
+          float hj[8];
+          if (LAYER == 1) {
+            const float rj = P::flt(r[j]) * inv_sigma, lj = g.node_lk[j];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) hj[t] = bf16r(fmaxf(fmaf(ew0[t], rj, fmaf(ew1[t], lj, eb[t])), 0.f));
+          } else {
+            unpack8(h_in[(int64_t)j * 4 + part], hj);
+          }
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            accA[t] = fmaf(ef.x, hj[t], accA[t]);
+            accL[t] = fmaf(ef.y, hj[t], accL[t]);
+          }
+        }
+        *reinterpret_cast<uint4 *>(sU + sU_off(m, part)) = pack8(hs);
+        *reinterpret_cast<uint4 *>(sU + sU_off(m, 4 + part)) = pack8(accA);
+        *reinterpret_cast<uint4 *>(sU + sU_off(m, 8 + part)) = pack8(accL);
+      }
+      // ---- 2. MLP on the tensor cores
+      fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t ua = smem_u32(sU), wa = smem_u32(sW);
+#pragma unroll
+        for (int k = 0; k < kIn / 16; ++k)
+          mma_bf16(tmem, mma_desc(ua + k * 2 * kCoreBytes), mma_desc(wa + k * 2 * kCoreBytes), k > 0 ? 1u : 0u);
+        mma_commit(&s_mbar);
+      }
+      bool ok = false;
+      for (int tries = 0; tries < kWaitLimit && !ok; ++tries) ok = mbar_try_wait(&s_mbar, phase);
+      if (!ok) s_err = 1;
+      phase ^= 1u;
+      tc_fence_after();
+      __syncthreads();
+      if (s_err) {
+        stop = true;
+        break;
+      }
+      // ---- 3. epilogue: row tid of the tile
+      float acc[32];
+      tmem_ld32(tmem_warp, acc);
+      const int64_t i = s0 + tid;
+      float o[32];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        float hv[8];
+        unpack8(*reinterpret_cast<const uint4 *>(sU + sU_off(tid, cc)), hv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int ch = 8 * cc + k;
+          o[ch] = bf16r(hv[k] + fmaxf(acc[ch] + sBias[ch], 0.f));
+        }
+      }
+      if (LAYER < 4) {
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          float f8[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) f8[k] = o[8 * cc + k];
+          h_out[i * 4 + cc] = pack8(f8);
+        }
+      } else {
+        float y = g.dec_b;
+#pragma unroll
+        for (int ch = 0; ch < kHid; ++ch) y = fmaf(sDec[ch], o[ch], y);
+        V zi = P::zero();
+        const V ri = r[i];
+        if (i < real_end) {
+          const V d = invdiag[i];
+          zi = P::fma(d, ri, P::mul(d, P::off(sigma * y)));
+        }
+        z[i] = zi;
+        zr.add(zi, ri);
+        zq.add(zi, q[i]);
+      }
+      tc_fence_before();
+      __syncthreads();  // sU and the accumulator are reused by the next tile
+    }
+    if (stop) break;
+    if (LAYER == 4) {
+      const double v[2] = {zr.value(), zq.value()};
+      double tot[2];
+      if (chunk_finish<2, kGThreads>(a, c, inst, v, L, tot) && tid == 0) {
+        esr_bcg_inst &s = L.inst[inst];
+        if (!(tot[0] > 0.0) || !isfinite(tot[0]) || !isfinite(tot[1]) || s.rz == 0.0) {
+          // the network's direction is unusable: Jacobi from here on
+          s.mode = kModeJacobi;
+          s.refresh = 1;
+          s.fallbacks += 1;
+          s.beta = 0.0;
+          s.rz = s.rz_jac;
+        } else {
+          s.beta = -s.alpha * tot[1] / s.rz;
+          s.rz = tot[0];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kTmemCols);
+  }
+  if (tid == 0 && s_err) esr::raise_status(ESR_DEV_WAIT_TIMEOUT);
+}
+
+template <class P>
+int launch_layers(const esr_batch *B, const void *r, const void *q, void *z, void *ws, cudaStream_t s) {
+  using V = typename P::V;
+  const esr_gnn *G = B->gnn;
+  BcgLayout L = layout_of(ws, B->ninst, B->nchunks);
+  const BArgs a = bargs(B);
+  const GArgs g{G->node_lk, reinterpret_cast<const float2 *>(G->edge_feat), G->enc_w, G->enc_b, G->layer_w,
+                G->layer_b, G->dec_w, G->dec_b};
+  const uint4 *h0 = (const uint4 *)G->h0;
+  const uint4 *h1 = (const uint4 *)G->h1;
+  const V *rv = (const V *)r, *qv = (const V *)q, *dv = (const V *)B->invdiag;
+  gnn_layer_kernel<1, P><<<G->grid, kGThreads, 0, s>>>(a, g, rv, qv, dv, (V *)z, nullptr, (uint4 *)G->h0, L);
+  gnn_layer_kernel<2, P><<<G->grid, kGThreads, 0, s>>>(a, g, rv, qv, dv, (V *)z, h0, (uint4 *)G->h1, L);
+  gnn_layer_kernel<3, P><<<G->grid, kGThreads, 0, s>>>(a, g, rv, qv, dv, (V *)z, h1, (uint4 *)G->h0, L);
+  gnn_layer_kernel<4, P><<<G->grid, kGThreads, 0, s>>>(a, g, rv, qv, dv, (V *)z, h0, nullptr, L);
+  ESR_LAUNCH_CHECK("esr_bcg_iterate/gnn");
+  return ESR_OK;
+}
+
+}  // namespace
+
+ESR_DEFINE_STATUS_READER(esr_status_gnn)
+
+namespace esr {
+int gnn_layers(const esr_batch *B, const void *r, const void *q, void *z, void *workspace, cudaStream_t s) {
+  return B->df64 ? launch_layers<PolDF>(B, r, q, z, workspace, s) : launch_layers<PolF64>(B, r, q, z, workspace, s);
+}
+}  // namespace esr

@@ -45,6 +45,7 @@ class LinsysInstance:
     Av: object
     b: object
     x0: object = None
+    edge_len: object = None  # per coupling, grid units (GNN edge input); 1 when None
 
 
 def _np(a, dtype):
@@ -73,7 +74,7 @@ class PackedBatch:
     with row/slot offsets.  Entries of a row keep the reference's edge order
     (stable sort of the Reducer index)."""
 
-    def __init__(self, instances: Sequence[LinsysInstance]):
+    def __init__(self, instances: Sequence[LinsysInstance], edge_features: bool = False):
         if len(instances) == 0:
             raise ValueError("empty batch")
         nblk = [max(1, -(-int(s.n) // ROWS_PER_BLOCK)) for s in instances]
@@ -85,7 +86,8 @@ class PackedBatch:
         self.n = self.nblocks * ROWS_PER_BLOCK
         self.row0 = self.inst_block0[:-1].astype(np.int64) * ROWS_PER_BLOCK
         self.block_inst = np.repeat(np.arange(self.ninst, dtype=np.int32), nblk)
-        sp_parts, col_parts, val_parts = [], [], []
+        sp_parts, col_parts, val_parts, w_parts, len_parts = [], [], [], [], []
+        self.node_lk = np.zeros(self.n, np.float32) if edge_features else None
         self.diag = np.ones(self.n, np.float64)
         self.b = np.zeros(self.n, np.float64)
         self.x0 = np.zeros(self.n, np.float64)
@@ -103,6 +105,18 @@ class PackedBatch:
             sp_parts.append(slice_ptr[:-1] + base)
             col_parts.append(np.where(c >= 0, c + r0, -1).astype(np.int32))
             val_parts.append(val)
+            if edge_features:
+                from .preconditioner.gnn import node_input
+                widths = np.diff(slice_ptr) // 32
+                srow = (np.repeat(np.arange(len(widths), dtype=np.int64) * 32, widths * 32)
+                        + np.arange(int(slice_ptr[-1]), dtype=np.int64) % 32)
+                cc = np.where(valid, c, 0)
+                rr = np.minimum(srow, max(n - 1, 0))
+                w = np.where(valid, val / np.sqrt(Av[rr] * Av[cc]) if n else 0.0, 0.0)
+                el = np.ones(len(val)) if s.edge_len is None else _np(s.edge_len, np.float64)[np.where(valid, src_pos, 0)]
+                w_parts.append(w.astype(np.float32))
+                len_parts.append(np.where(valid, el, 0.0).astype(np.float32))
+                self.node_lk[r0:r0 + n] = node_input(Av).astype(np.float32)
             base += int(slice_ptr[-1])
             self.diag[r0:r0 + n] = Av
             self.b[r0:r0 + n] = _np(s.b, np.float64)
@@ -113,6 +127,8 @@ class PackedBatch:
         self.slice_ptr = np.concatenate(sp_parts + [np.array([base], np.int64)])
         self.col = np.concatenate(col_parts)
         self.val = np.concatenate(val_parts)
+        self.edge_feat = (np.stack([np.concatenate(w_parts), np.concatenate(len_parts)], axis=1)
+                          if edge_features else None)
 
     def rows(self, i: int) -> slice:
         r0 = int(self.row0[i])
@@ -148,13 +164,15 @@ class BatchedPCG:
 
     def __init__(self, instances: Sequence[LinsysInstance], jacobi: bool = True, precision: str = "df64",
                  device="cuda", graph_iters: int = 32, use_graph: bool = True, tiles_per_chunk: int = 4,
-                 grid: Optional[int] = None):
+                 grid: Optional[int] = None, gnn=None, stall_window: int = 32, gnn_ctas_per_sm: int = 4):
         if precision not in ("fp64", "df64"):
             raise ValueError("precision must be 'fp64' or 'df64'")
         dev = torch.device(device)
         if dev.type != "cuda":
             raise ValueError("BatchedPCG runs on a CUDA device")
-        pk = PackedBatch(instances)
+        if gnn is not None and not jacobi:
+            raise ValueError("the GNN preconditioner falls back to Jacobi: jacobi must be True")
+        pk = PackedBatch(instances, edge_features=gnn is not None)
         self.pack = pk
         self.dev = dev
         self.precision = precision
@@ -189,6 +207,19 @@ class BatchedPCG:
         self.kernel_launches = 0
         self.polls = 0
         self.tuning = None
+        self.gnn_desc = None
+        if gnn is not None:
+            self._gnn = gnn.device_tensors(dev)
+            self._gnn["node_lk"] = t(pk.node_lk)
+            self._gnn["edge_feat"] = t(pk.edge_feat)
+            self._gnn["inst_rows"] = t(pk.sizes.astype(np.int32))
+            self._gnn["h0"] = torch.zeros(n * 32, dtype=torch.bfloat16, device=dev)
+            self._gnn["h1"] = torch.zeros(n * 32, dtype=torch.bfloat16, device=dev)
+            g = self._gnn
+            self.gnn_desc = _lib.Gnn(_lib.ptr(g["node_lk"]), _lib.ptr(g["edge_feat"]), _lib.ptr(g["inst_rows"]),
+                                     _lib.ptr(g["h0"]), _lib.ptr(g["h1"]), _lib.ptr(g["enc_w"]), _lib.ptr(g["enc_b"]),
+                                     _lib.ptr(g["layer_w"]), _lib.ptr(g["layer_b"]), _lib.ptr(g["dec_w"]),
+                                     float(gnn.dec_b), int(gnn_ctas_per_sm * self.sm_count), int(stall_window), 0)
         self.set_shape(tiles_per_chunk, grid if grid is not None else 4 * self.sm_count)
 
     def set_shape(self, tiles_per_chunk: int, grid: int):
@@ -207,7 +238,8 @@ class BatchedPCG:
                                _lib.ptr(self.val), _lib.ptr(self.diag), _lib.ptr(self.invdiag),
                                _lib.ptr(self.val64), _lib.ptr(self.diag64), _lib.ptr(self.block_inst),
                                _lib.ptr(self.inst_block0), _lib.ptr(self.chunk_tile0), _lib.ptr(self.chunk_inst),
-                               _lib.ptr(self.inst_chunk0))
+                               _lib.ptr(self.inst_chunk0),
+                               ctypes.pointer(self.gnn_desc) if self.gnn_desc is not None else None)
         self._graphs = {}
 
     def bytes_per_row_iteration(self) -> float:
@@ -286,7 +318,8 @@ class BatchedPCG:
             self.x[rows] = conv(x0.to(self.dev, torch.float64))
 
     # ---------------------------------------------------------- autotune --
-    def autotune(self, tiles=(1, 2, 4, 8, 16), ctas_per_sm=(2, 3, 4, 6, 8), iters: int = 8, reps: int = 2) -> dict:
+    def autotune(self, tiles=(2, 4, 8, 16, 32, 64), ctas_per_sm=(2, 3, 4, 6, 8), iters: int = 8,
+                 reps: int = 2) -> dict:
         """Times ``iters`` lockstep iterations (every instance running) for
         each (tiles per chunk, persistent CTAs per SM) pair on this batch and
         keeps the fastest.  Leaves x untouched; the next ``run`` starts from
@@ -330,6 +363,17 @@ class BatchedPCG:
                   -1 if maxiter is None else int(maxiter), _lib.ptr(self.ws), self._stream())
         self.kernel_launches += 1
 
+    def apply_preconditioner(self, r: torch.Tensor, z: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """z = M(r) with the GNN preconditioner for every instance (packed
+        vectors in the engine's precision); overwrites the solver state."""
+        if self.gnn_desc is None:
+            raise ValueError("no GNN preconditioner attached")
+        z = torch.empty_like(r) if z is None else z
+        _lib.call("esr_gnn_apply", ctypes.byref(self.desc), _lib.ptr(r), _lib.ptr(z), _lib.ptr(self.ws),
+                  self._stream())
+        self.kernel_launches += 6
+        return z
+
     def verify(self):
         _lib.call("esr_bcg_verify", ctypes.byref(self.desc), _lib.ptr(self.b64), _lib.ptr(self.x),
                   _lib.ptr(self.x64), _lib.ptr(self.r64), _lib.ptr(self.r), _lib.ptr(self.z), _lib.ptr(self.p),
@@ -351,6 +395,11 @@ class BatchedPCG:
             self.verify()
             rounds += 1
             if self.active() == 0 or rounds >= max_rounds:
+                if self.gnn_desc is not None:
+                    from .. import ops
+                    bits = ops.device_status(clear=True)
+                    if bits & _lib.DEV_WAIT_TIMEOUT:
+                        raise RuntimeError("a GNN tensor-core wait timed out on the device")
                 return rounds
 
     def solve(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: Optional[int] = None,
@@ -369,7 +418,8 @@ class BatchedPCG:
             status = "unverified"
         tr = float(s.true_rr) ** 0.5 if s.true_rr >= 0 else float("nan")
         return {"status": status, "iters": max(int(s.iters) - 1, 0), "residual": float(s.rr) ** 0.5,
-                "true_residual": tr, "bnorm": float(s.bnorm), "tol": float(s.tol), "restarts": int(s.restarts)}
+                "true_residual": tr, "bnorm": float(s.bnorm), "tol": float(s.tol), "restarts": int(s.restarts),
+                "mode": "gnn" if s.mode == 1 else "jacobi", "fallbacks": int(s.fallbacks)}
 
     def solution(self, i: Optional[int] = None) -> torch.Tensor:
         """FP64 solution of instance i (all packed rows when None)."""
@@ -393,5 +443,14 @@ def p1_instances(count: int, nmin: int, nmax: int, seed: int = 0, corr_len: floa
         kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, seed * 100_003 + 2 * i, corr_len, variance))
         s = mesh.p1_system(n, kappa)
         b = mesh.random_mode_rhs(n, seed * 100_003 + 2 * i + 1)
-        out.append(LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, b))
+        out.append(LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, b, edge_len=p1_edge_length(n, s.row, s.col)))
     return out
+
+
+def p1_edge_length(n: int, row: np.ndarray, col: np.ndarray) -> np.ndarray:
+    """Length (grid units) of each coupling of the P1 grid system: unknown
+    u = (j-1)*(n-1) + (i-1) sits at node (i, j)."""
+    m = max(n - 1, 1)
+    di = (col % m) - (row % m)
+    dj = (col // m) - (row // m)
+    return np.sqrt((di * di + dj * dj).astype(np.float64))

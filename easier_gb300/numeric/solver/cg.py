@@ -118,6 +118,7 @@ class CG(esr.Module):
                 inst = LinsysInstance(n, A.reducer.idx.detach().cpu().numpy(), A.selector.idx.detach().cpu().numpy(),
                                       A.Ae.data, A.Av.data, self.b.data)
                 self._fused = BatchedPCG([inst], jacobi=jacobi, precision="df64", device=self.x.device)
+                self._fused.autotune()
             else:
                 self._fused = FusedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
             self._fused_key = key

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 3
+#define ESR_GB300_ABI_VERSION 4
 
 /* element types */
 enum {
@@ -66,7 +66,8 @@ enum {
 /* device-side error bits, OR-ed into the library's device status word */
 enum {
   ESR_DEV_IDX_RANGE = 1,  /* an index was outside [0, n_in)                */
-  ESR_DEV_NONFINITE = 2   /* a solver produced NaN/Inf                     */
+  ESR_DEV_NONFINITE = 2,  /* a solver produced NaN/Inf                     */
+  ESR_DEV_WAIT_TIMEOUT = 4 /* a bounded device wait gave up                */
 };
 
 const char *esr_last_error(void);
@@ -448,6 +449,34 @@ int esr_axpy_f64(double *x, int dtype_d, const void *d, double scale,
  *           hi + lo), the arithmetic runs on the FP32 pipes with ~48
  *           significand bits; val64/diag64 (FP64) serve the true-residual
  *           check of esr_bcg_verify. */
+/* GNN preconditioner of the batched flexible CG (no reference counterpart).
+ * Per node i of an instance, with sigma = rms of the instance's residual:
+ *   h0_i = relu(enc_w [r_i / sigma, lk_i] + enc_b)                  (32)
+ *   4 layers l: A_i = sum_j w_ij h_j, L_i = sum_j len_ij h_j over the
+ *     SELL slots of row i; h_i += relu(W_l [h_i, A_i, L_i] + b_l)     (96 -> 32)
+ *   y_i = dec_w . h_i + dec_b;  z_i = invdiag_i (r_i + sigma y_i)
+ * h and the MLP inputs are BF16, the MLP runs on the tensor cores
+ * (tcgen05, FP32 accumulation in tensor memory), aggregation in FP32.
+ * Instances fall back to Jacobi (z = invdiag r, direction restart) when the
+ * preconditioned direction breaks down (z.r <= 0) or the residual has not
+ * decreased over `stall_window` iterations. */
+typedef struct {
+  const float *node_lk;     /* [n] node input (log kappa); 0 on padding rows */
+  const float *edge_feat;   /* [nslots][2] (w, len) per SELL slot            */
+  const int32_t *inst_rows; /* [ninst] rows of each instance before padding  */
+  void *h0;                 /* [n][32] BF16 scratch                          */
+  void *h1;                 /* [n][32] BF16 scratch                          */
+  const float *enc_w;       /* [32][2]                                       */
+  const float *enc_b;       /* [32]                                          */
+  const uint16_t *layer_w;  /* [4][32][96] BF16 bits, [out][in]              */
+  const float *layer_b;     /* [4][32]                                       */
+  const float *dec_w;       /* [32]                                          */
+  float dec_b;
+  int32_t grid;             /* persistent CTAs of the GNN layer kernels      */
+  int32_t stall_window;     /* iterations                                    */
+  int32_t pad_;
+} esr_gnn;
+
 typedef struct {
   int64_t n;               /* packed rows = 256 * nblocks                  */
   int32_t ninst;
@@ -468,17 +497,26 @@ typedef struct {
   const int32_t *chunk_tile0;/* [nchunks + 1] first tile of each chunk     */
   const int32_t *chunk_inst; /* [nchunks] instance of each chunk           */
   const int32_t *inst_chunk0;/* [ninst + 1] first chunk of each instance   */
+  const esr_gnn *gnn;        /* NULL: Jacobi (or no) PCG; else flexible CG
+                                with the GNN preconditioner                */
 } esr_batch;
 
 /* Per-instance device scalars. */
 typedef struct {
   double rz, pq, alpha, beta, rr, bnorm, tol;
   double true_rr;    /* FP64 ||b - A x||^2 of the last verification, -1 none */
+  double sigma;      /* rms of r (GNN input scale)                          */
+  double rr_mark;    /* r.r at the last stall check                         */
+  double rz_jac;     /* r.(invdiag r) of the current residual               */
   int32_t iters;     /* completed step() calls                              */
   int32_t done;      /* 0 running, 1 converged, 2 maxiter, 3 breakdown/NaN  */
   int32_t verified;  /* 1 = FP64 true residual <= tol                       */
   int32_t restarts;  /* residual replacements after a failed verification   */
   int32_t maxiter;
+  int32_t mode;      /* 0 Jacobi, 1 GNN                                     */
+  int32_t refresh;   /* 1: next p-update restarts with p = invdiag r        */
+  int32_t fallbacks; /* GNN -> Jacobi switches                              */
+  int32_t nrows;     /* rows before padding                                 */
   int32_t pad_;
 } esr_bcg_inst;
 
@@ -506,6 +544,12 @@ int esr_bcg_iterate(const esr_batch *B, void *x, void *r, void *z, void *p,
 int esr_bcg_verify(const esr_batch *B, const double *b64, void *x, double *x64,
                    double *r64, void *r, void *z, void *p, void *workspace,
                    void *stream);
+
+/* The GNN preconditioner alone: z = M(r) for every instance of a batch
+ * with batch.gnn set (sigma = rms of each instance's r), zero on padding
+ * rows.  Uses (and overwrites) the workspace.  6 launches. */
+int esr_gnn_apply(const esr_batch *B, const void *r, void *z, void *workspace,
+                  void *stream);
 
 /* Running-instance count and (if inst_out) the per-instance scalars, to
  * host memory; synchronises `stream`. */
