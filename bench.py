@@ -494,6 +494,71 @@ def bench_batched(args, world, rank, local):
     return line
 
 
+# ---------------------------------------------------- GNN-preconditioned --
+def bench_gnn(args, world, rank, local):
+    """Flexible CG with the GNN preconditioner against Jacobi-PCG, both
+    batched and df64, on held-out seeded instances."""
+    from easier_gb300.numeric.batched import BatchedPCG, p1_instances
+    from easier_gb300.numeric.preconditioner.gnn import GnnWeights, WEIGHTS_FILE
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for name, kw in (("jacobi", {}), ("gnn", {"gnn": GnnWeights.load()})):
+        eng = BatchedPCG(insts, jacobi=True, precision="df64", device=dev, graph_iters=args.chunk, **kw)
+        eng.autotune()
+        x0 = torch.zeros_like(eng.b64)
+        for _ in range(args.warmup):
+            eng.load_packed(x0=x0)
+            eng.run(1e-8)
+        torch.cuda.synchronize(dev)
+        l0 = eng.kernel_launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            _barrier(world)
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            for _ in range(args.steps):
+                eng.load_packed(x0=x0)
+                eng.run(1e-8)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            _barrier(world)
+        ms = _max_over_ranks(world, e0.elapsed_time(e1))
+        res = [eng._info(s) for s in eng.instances()]
+        bad = [r for r in res if r["status"] != "converged" or not r["true_residual"] <= 1e-8 * r["bnorm"] * 1.0001]
+        if bad:
+            raise RuntimeError(f"{name}: {len(bad)} instances not FP64-verified at 1e-8, e.g. {bad[0]}")
+        its = np.array([r["iters"] for r in res])
+        out[name] = {"solves_per_s": world * len(insts) / (ms / args.steps / 1e3), "ms_per_batch": ms / args.steps,
+                     "iters_mean": float(its.mean()), "iters_max": int(its.max()),
+                     "fallbacks": int(sum(r["fallbacks"] for r in res)),
+                     "theta_clips": int(sum(r["clips"] for r in res)),
+                     "launches_per_batch": (eng.kernel_launches - l0) // args.steps, "clocks": clk.summary()}
+        del eng
+        torch.cuda.empty_cache()
+    g, j = out["gnn"], out["jacobi"]
+    peak, peak_kind = _peaks()
+    return {
+        "metric": "Poisson solves/s (batched, GNN-preconditioned flexible CG)", "value": g["solves_per_s"],
+        "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": g["ms_per_batch"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "df64 (f32 pairs) CG, bf16 GNN with f32 accumulation",
+        "data": f"synthetic held-out instances (seed {args.seed}); weights {WEIGHTS_FILE.name}",
+        "config": {"workload": f"{len(insts)} P1 Poisson instances, N ~ U{{{args.nmin}..{args.nmax}}}, GRF kappa, "
+                               f"to FP64-verified rel. residual 1e-8",
+                   "gnn": {k: v for k, v in g.items() if k != "clocks"},
+                   "jacobi": {k: v for k, v in j.items() if k != "clocks"},
+                   "gnn_over_jacobi_solves_per_s": g["solves_per_s"] / j["solves_per_s"],
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                     "peak_kind": peak_kind, "traffic": None},
+        "gpu_launches": g["launches_per_batch"],
+        "clocks": g["clocks"],
+    }
+
+
 # ------------------------------------------------------------ reference --
 def bench_reference(args):
     """The reference's CPU algorithm (oracle) on the host cores."""
@@ -517,7 +582,7 @@ def bench_reference(args):
         unit, metric = "cell-steps/s", "SWE cell-steps/s"
         sample = f"{args.steps} full oracle steps at N={args.n} ({m.nc} cells), {args.dtype}"
         cfg = {"workload": f"shallow water, tutorial mesh N={args.n} ({m.nc} cells, {m.ne} directed edges), dt={args.dt}"}
-    elif args.workload == "batched":
+    elif args.workload in ("batched", "gnn"):
         from easier_gb300.numeric.batched import p1_instances
         from oracle import cg as ocg
         insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
@@ -567,11 +632,11 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["swe", "poisson", "batched"], default="swe")
+    ap.add_argument("--workload", choices=["swe", "poisson", "batched", "gnn"], default="swe")
     ap.add_argument("--count", type=int, default=256, help="batched: instances")
     ap.add_argument("--nmin", type=int, default=32, help="batched: smallest mesh side")
     ap.add_argument("--nmax", type=int, default=512, help="batched: largest mesh side")
-    ap.add_argument("--seed", type=int, default=0, help="batched: instance seed")
+    ap.add_argument("--seed", type=int, default=None, help="batched: instance seed (gnn: held-out seed 1)")
     ap.add_argument("--chunk", type=int, default=32, help="batched: iterations per CUDA graph")
     ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default work shape")
     ap.add_argument("--n", type=int, default=None)
@@ -592,18 +657,20 @@ def main():
         args.dt = 5e-4 if args.n <= 1000 else 2.5e-4
     if args.precision is None:
         args.precision = "fast" if args.workload == "swe" else "native"
+    if args.seed is None:
+        args.seed = 1 if args.workload == "gnn" else 0
     world, rank, local = _dist()
     if args.impl == "reference":
         if args.steps is None:
-            args.steps = {"swe": 3, "poisson": 1, "batched": 4}[args.workload]
+            args.steps = {"swe": 3, "poisson": 1, "batched": 4, "gnn": 4}[args.workload]
         if args.warmup is None:
-            args.warmup = {"swe": 1, "poisson": 0, "batched": 1}[args.workload]
+            args.warmup = {"swe": 1, "poisson": 0, "batched": 1, "gnn": 1}[args.workload]
         if rank != 0:
             return
         print(json.dumps(bench_reference(args)), flush=True)
         return
     if args.steps is None:
-        args.steps = {"swe": 1000, "poisson": 10, "batched": 5}[args.workload]
+        args.steps = {"swe": 1000, "poisson": 10, "batched": 5, "gnn": 3}[args.workload]
     if args.warmup is None:
         args.warmup = 10 if args.workload == "swe" else 3
     if args.warmup < 3:
@@ -611,7 +678,7 @@ def main():
     if world > 1:
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    run = {"swe": bench_swe, "poisson": bench_poisson, "batched": bench_batched}[args.workload]
+    run = {"swe": bench_swe, "poisson": bench_poisson, "batched": bench_batched, "gnn": bench_gnn}[args.workload]
     line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -69,10 +69,10 @@ class Batch(Structure):
 class BcgInst(Structure):
     _fields_ = [("rz", c_double), ("pq", c_double), ("alpha", c_double), ("beta", c_double),
                 ("rr", c_double), ("bnorm", c_double), ("tol", c_double), ("true_rr", c_double),
-                ("sigma", c_double), ("rr_mark", c_double), ("rz_jac", c_double),
+                ("sigma", c_double), ("rr_mark", c_double), ("rz_jac", c_double), ("theta", c_double),
                 ("iters", c_int32), ("done", c_int32), ("verified", c_int32), ("restarts", c_int32),
                 ("maxiter", c_int32), ("mode", c_int32), ("refresh", c_int32), ("fallbacks", c_int32),
-                ("nrows", c_int32), ("pad_", c_int32)]
+                ("nrows", c_int32), ("gnn_iters", c_int32), ("clips", c_int32), ("clips_mark", c_int32)]
 
 
 _P = c_void_p

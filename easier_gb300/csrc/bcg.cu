@@ -107,6 +107,10 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     s.mode = a.use_gnn ? kModeGnn : kModeJacobi;
     s.refresh = 0;
     s.fallbacks = 0;
+    s.gnn_iters = 0;
+    s.clips = 0;
+    s.clips_mark = 0;
+    s.theta = 1.0;
     s.nrows = a.use_gnn ? a.inst_rows[inst] : 0;
     s.sigma = s.nrows > 0 ? sqrt(tot[2] / s.nrows) : 0.0;
     s.rr_mark = tot[2];
@@ -201,10 +205,13 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
         // the stall test (no decrease of r.r over a window -> Jacobi)
         s.sigma = s.nrows > 0 ? sqrt(tot[0] / s.nrows) : 0.0;
         if (a.stall_window > 0 && s.iters % a.stall_window == 0) {
-          if (!(tot[0] < s.rr_mark)) {
+          const bool clipped = 2 * (s.clips - s.clips_mark) > a.stall_window;
+          s.clips_mark = s.clips;
+          if (!(tot[0] < s.rr_mark) || clipped) {
             s.mode = kModeJacobi;
             s.refresh = 1;
             s.fallbacks += 1;
+            s.gnn_iters = s.iters;
             s.beta = 0.0;
             s.rz = tot[1];
           } else {
@@ -233,13 +240,20 @@ bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, const typename 
     if (L.inst[inst].done) continue;
     const V beta = P::of(L.inst[inst].beta);
     const bool refresh = L.inst[inst].refresh != 0;
+    const double theta = L.inst[inst].theta;
+    const bool blend = L.inst[inst].mode == kModeGnn && theta != 1.0;
+    const V th = P::of(theta), omth = P::of(1.0 - theta);
     const int t1 = a.chunk_tile0[c + 1];
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
       const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
-      if (refresh)
+      if (refresh) {
         p[i] = invdiag ? P::mul(r[i], invdiag[i]) : r[i];
-      else
+      } else if (blend) {  // z = (1 - theta) invdiag r + theta z_network
+        const V zb = P::fma(th, z[i], P::mul(omth, P::mul(r[i], invdiag[i])));
+        p[i] = P::fma(beta, p[i], zb);
+      } else {
         p[i] = P::fma(beta, p[i], z[i]);
+      }
     }
   }
 }

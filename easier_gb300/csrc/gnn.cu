@@ -4,7 +4,8 @@
 //
 // One launch per layer.  Each is persistent over the active chunk list of
 // the batch and walks a chunk in 128-node tiles:
-//   1. aggregation (CUDA cores, FP32): 4 threads per node, 8 channels each,
+//   1. aggregation (CUDA cores, FP32): 4 threads per node (512 threads, one
+//      pass per tile), 8 channels each,
 //      gather the neighbours' BF16 features over the node's SELL slots and
 //      form u = [h_i, sum_j w_ij h_j, sum_j len_ij h_j] (96 BF16) in shared
 //      memory, in the K-major core-matrix layout of the MMA (8 rows x 16 B
@@ -13,11 +14,13 @@
 //   2. one thread issues 6 tcgen05.mma (M=128, N=32, K=16 each, BF16 in,
 //      FP32 accumulate) against the layer's weights, staged once per CTA in
 //      the same layout, and commits to an mbarrier;
-//   3. every warp reads its 32 accumulator lanes (tcgen05.ld 32x32b.x32),
-//      adds bias, ReLU and the residual h_i and stores BF16 h (layers 1-3),
+//   3. each of the 16 warps reads 8 accumulator columns of the 32 lanes it
+//      may access (tcgen05.ld 32x32b.x8), adds bias, ReLU and the residual
+//      h_i and stores BF16 h (layers 1-3),
 //      or (layer 4) decodes y_i = dec_w . h_i + dec_b and writes
-//      z_i = invdiag_i (r_i + sigma y_i), accumulating z.r and z.q for the
-//      instance's Polak-Ribiere beta.
+//      z_i = invdiag_i (r_i + sigma y_i), accumulating the dots that fix the
+//      instance's correction weight theta (z.r >= half the Jacobi r.z; the
+//      p-update applies theta) and its Polak-Ribiere beta.
 // Layer 1 evaluates the encoder h0 = relu(enc_w [r/sigma, lk] + enc_b) on
 // the fly for the node and its neighbours instead of storing h0.
 //
@@ -29,7 +32,7 @@
 
 namespace {
 
-constexpr int kGThreads = 128;                    // CTA threads
+constexpr int kGThreads = 512;                    // CTA threads: 4 per node of a tile
 constexpr int kGRows = 128;                       // nodes per MMA tile (M)
 constexpr int kHid = 32;                          // hidden width (N)
 constexpr int kIn = 96;                           // MLP input (K) = [h, A, L]
@@ -39,7 +42,8 @@ constexpr int kSBO = kKChunks * kCoreBytes;       // bytes between 8-row groups
 constexpr uint32_t kTmemCols = 32;                // FP32 accumulator columns
 constexpr int kWaitLimit = 1 << 22;               // mbarrier polls before giving up
 
-static_assert(kGThreads == kGRows, "one accumulator row per thread");
+static_assert(kGThreads == 4 * kGRows, "4 aggregation threads per node");
+static_assert(kGThreads / 32 == 4 * (kHid / 8), "16 warps: 4 TMEM lane groups x 4 column groups");
 static_assert(kBThreads % kGRows == 0, "tiles split into whole MMA tiles");
 
 // instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16 (bits 7-9
@@ -108,20 +112,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// 32 consecutive FP32 accumulator columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
+// 8 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
 }
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
@@ -152,7 +151,7 @@ __device__ __forceinline__ void unpack8(uint4 u, float (&f)[8]) {
 __device__ __forceinline__ int sU_off(int m, int chunk) { return (m >> 3) * kSBO + chunk * kCoreBytes + (m & 7) * 16; }
 
 template <int LAYER, class P>
-__global__ void __launch_bounds__(kGThreads)
+__global__ void __launch_bounds__(kGThreads, 2)
 gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const typename P::V *__restrict__ q,
                  const typename P::V *__restrict__ invdiag, typename P::V *__restrict__ z,
                  const uint4 *__restrict__ h_in, uint4 *__restrict__ h_out, BcgLayout L) {
@@ -161,12 +160,18 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
   __shared__ __align__(1024) uint8_t sW[kHid * kIn * 2];
   __shared__ float sBias[kHid];
   __shared__ float sDec[kHid];
+  __shared__ float sY[kHid / 8][kGRows];  // layer 4: decoder partial sums per channel group
   __shared__ __align__(8) uint64_t s_mbar;
   __shared__ uint32_t s_tmem;
   __shared__ int s_err;
 
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int part = tid & 3;  // aggregation: channels 8*part .. 8*part+7
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // aggregation: node m_agg, channels 8*part .. 8*part+7
+  const int m_agg = tid >> 2, part = tid & 3;
+  // epilogue: TMEM lanes 32*(warp%4) (the lanes this warp may read), row
+  // m_epi of the tile, accumulator columns 8*cgrp .. 8*cgrp+7
+  const int lgrp = warp & 3, cgrp = warp >> 2;
+  const int m_epi = 32 * lgrp + lane;
   {
     const uint16_t *W = g.layer_w + (LAYER - 1) * kHid * kIn;
     for (int e = tid; e < kHid * kKChunks; e += kGThreads) {
@@ -191,7 +196,7 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
-  const uint32_t tmem_warp = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t tmem_epi = tmem + ((uint32_t)(32 * lgrp) << 16) + (uint32_t)(8 * cgrp);
 
   float ew0[8], ew1[8], eb[8];  // encoder rows of this thread's channels
   if (LAYER == 1) {
@@ -201,6 +206,12 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
       ew1[k] = g.enc_w[(8 * part + k) * 2 + 1];
       eb[k] = g.enc_b[8 * part + k];
     }
+  }
+  float bias[8], dec[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    bias[k] = sBias[8 * cgrp + k];
+    dec[k] = sDec[8 * cgrp + k];
   }
 
   uint32_t phase = 0;
@@ -213,15 +224,13 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
     const float sigma = (float)st.sigma;
     const float inv_sigma = sigma > 0.f ? 1.f / sigma : 0.f;
     const int64_t real_end = (int64_t)a.inst_block0[inst] * kBThreads + st.nrows;
-    typename P::Acc zr, zq;
+    typename P::Acc nr, nq, jq;  // zN.r, zN.q, zJ.q (zJ = invdiag r, zN = invdiag sigma y)
     const int64_t row1 = (int64_t)a.chunk_tile0[c + 1] * kBThreads;
     bool stop = false;
     for (int64_t s0 = (int64_t)a.chunk_tile0[c] * kBThreads; s0 < row1; s0 += kGRows) {
-      // ---- 1. aggregation into sU
-#pragma unroll 1
-      for (int pass = 0; pass < kGRows / 32; ++pass) {
-        const int m = pass * 32 + (tid >> 2);
-        const int64_t i = s0 + m;
+      // ---- 1. aggregation into sU: 4 threads per node, one node per quad
+      {
+        const int64_t i = s0 + m_agg;
         float hs[8], accA[8], accL[8];
         if (LAYER == 1) {
           const float rh = P::flt(r[i]) * inv_sigma, lk = g.node_lk[i];
@@ -255,9 +264,9 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
             accL[t] = fmaf(ef.y, hj[t], accL[t]);
           }
         }
-        *reinterpret_cast<uint4 *>(sU + sU_off(m, part)) = pack8(hs);
-        *reinterpret_cast<uint4 *>(sU + sU_off(m, 4 + part)) = pack8(accA);
-        *reinterpret_cast<uint4 *>(sU + sU_off(m, 8 + part)) = pack8(accL);
+        *reinterpret_cast<uint4 *>(sU + sU_off(m_agg, part)) = pack8(hs);
+        *reinterpret_cast<uint4 *>(sU + sU_off(m_agg, 4 + part)) = pack8(accA);
+        *reinterpret_cast<uint4 *>(sU + sU_off(m_agg, 8 + part)) = pack8(accL);
       }
       // ---- 2. MLP on the tensor cores
       fence_async_smem();
@@ -280,62 +289,70 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
         stop = true;
         break;
       }
-      // ---- 3. epilogue: row tid of the tile
-      float acc[32];
-      tmem_ld32(tmem_warp, acc);
-      const int64_t i = s0 + tid;
-      float o[32];
-#pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
+      // ---- 3. epilogue: row m_epi, channels 8*cgrp .. 8*cgrp+7
+      float acc[8];
+      tmem_ld8(tmem_epi, acc);
+      const int64_t i = s0 + m_epi;
+      float o[8];
+      {
         float hv[8];
-        unpack8(*reinterpret_cast<const uint4 *>(sU + sU_off(tid, cc)), hv);
+        unpack8(*reinterpret_cast<const uint4 *>(sU + sU_off(m_epi, cgrp)), hv);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int ch = 8 * cc + k;
-          o[ch] = bf16r(hv[k] + fmaxf(acc[ch] + sBias[ch], 0.f));
-        }
+        for (int k = 0; k < 8; ++k) o[k] = bf16r(hv[k] + fmaxf(acc[k] + bias[k], 0.f));
       }
       if (LAYER < 4) {
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-          float f8[8];
-#pragma unroll
-          for (int k = 0; k < 8; ++k) f8[k] = o[8 * cc + k];
-          h_out[i * 4 + cc] = pack8(f8);
-        }
+        h_out[i * 4 + cgrp] = pack8(o);
       } else {
-        float y = g.dec_b;
+        float yp = 0.f;
 #pragma unroll
-        for (int ch = 0; ch < kHid; ++ch) y = fmaf(sDec[ch], o[ch], y);
-        V zi = P::zero();
-        const V ri = r[i];
-        if (i < real_end) {
-          const V d = invdiag[i];
-          zi = P::fma(d, ri, P::mul(d, P::off(sigma * y)));
+        for (int k = 0; k < 8; ++k) yp = fmaf(dec[k], o[k], yp);
+        sY[cgrp][m_epi] = yp;
+        __syncthreads();
+        if (cgrp == 0) {
+          const float y = g.dec_b + ((sY[0][m_epi] + sY[1][m_epi]) + (sY[2][m_epi] + sY[3][m_epi]));
+          V zi = P::zero();
+          const V ri = r[i], qi = q[i];
+          if (i < real_end) {
+            const V d = invdiag[i];
+            const V zn = P::mul(d, P::off(sigma * y));
+            const V zj = P::mul(d, ri);
+            zi = P::fma(d, ri, zn);
+            nr.add(zn, ri);
+            nq.add(zn, qi);
+            jq.add(zj, qi);
+          }
+          z[i] = zi;
         }
-        z[i] = zi;
-        zr.add(zi, ri);
-        zq.add(zi, q[i]);
       }
       tc_fence_before();
-      __syncthreads();  // sU and the accumulator are reused by the next tile
+      __syncthreads();  // sU, sY and the accumulator are reused by the next tile
     }
     if (stop) break;
     if (LAYER == 4) {
-      const double v[2] = {zr.value(), zq.value()};
-      double tot[2];
-      if (chunk_finish<2, kGThreads>(a, c, inst, v, L, tot) && tid == 0) {
+      const double v[3] = {nr.value(), nq.value(), jq.value()};
+      double tot[3];
+      if (chunk_finish<3, kGThreads>(a, c, inst, v, L, tot) && tid == 0) {
         esr_bcg_inst &s = L.inst[inst];
-        if (!(tot[0] > 0.0) || !isfinite(tot[0]) || !isfinite(tot[1]) || s.rz == 0.0) {
+        // z = zJ + theta zN with z.r >= zJ.r / 2 (zJ.r = rz_jac > 0)
+        const double jr = s.rz_jac;
+        double theta = 1.0;
+        if (tot[0] < -0.5 * jr) {
+          theta = 0.5 * jr / -tot[0];
+          s.clips += 1;
+        }
+        const double zr = jr + theta * tot[0], zq = tot[2] + theta * tot[1];
+        s.theta = theta;
+        if (!(zr > 0.0) || !isfinite(zr) || !isfinite(zq) || s.rz == 0.0) {
           // the network's direction is unusable: Jacobi from here on
           s.mode = kModeJacobi;
           s.refresh = 1;
           s.fallbacks += 1;
+          s.gnn_iters = s.iters;
           s.beta = 0.0;
           s.rz = s.rz_jac;
         } else {
-          s.beta = -s.alpha * tot[1] / s.rz;
-          s.rz = tot[0];
+          s.beta = -s.alpha * zq / s.rz;
+          s.rz = zr;
         }
       }
     }

@@ -164,7 +164,7 @@ class BatchedPCG:
 
     def __init__(self, instances: Sequence[LinsysInstance], jacobi: bool = True, precision: str = "df64",
                  device="cuda", graph_iters: int = 32, use_graph: bool = True, tiles_per_chunk: int = 4,
-                 grid: Optional[int] = None, gnn=None, stall_window: int = 32, gnn_ctas_per_sm: int = 4):
+                 grid: Optional[int] = None, gnn=None, stall_window: int = 64, gnn_ctas_per_sm: int = 2):
         if precision not in ("fp64", "df64"):
             raise ValueError("precision must be 'fp64' or 'df64'")
         dev = torch.device(device)
@@ -269,7 +269,7 @@ class BatchedPCG:
                   _lib.ptr(self.p), _lib.ptr(self.q), int(k), _lib.ptr(self.ws), self._stream())
 
     def _group(self, k: int):
-        self.kernel_launches += 1 + 3 * k
+        self.kernel_launches += 1 + (7 if self.gnn_desc is not None else 3) * k
         if not self.use_graph:
             self._iterate_call(k)
             return
@@ -419,7 +419,8 @@ class BatchedPCG:
         tr = float(s.true_rr) ** 0.5 if s.true_rr >= 0 else float("nan")
         return {"status": status, "iters": max(int(s.iters) - 1, 0), "residual": float(s.rr) ** 0.5,
                 "true_residual": tr, "bnorm": float(s.bnorm), "tol": float(s.tol), "restarts": int(s.restarts),
-                "mode": "gnn" if s.mode == 1 else "jacobi", "fallbacks": int(s.fallbacks)}
+                "mode": "gnn" if s.mode == 1 else "jacobi", "fallbacks": int(s.fallbacks),
+                "fallback_iter": int(s.gnn_iters), "clips": int(s.clips)}
 
     def solution(self, i: Optional[int] = None) -> torch.Tensor:
         """FP64 solution of instance i (all packed rows when None)."""

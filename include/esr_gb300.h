@@ -454,12 +454,16 @@ int esr_axpy_f64(double *x, int dtype_d, const void *d, double scale,
  *   h0_i = relu(enc_w [r_i / sigma, lk_i] + enc_b)                  (32)
  *   4 layers l: A_i = sum_j w_ij h_j, L_i = sum_j len_ij h_j over the
  *     SELL slots of row i; h_i += relu(W_l [h_i, A_i, L_i] + b_l)     (96 -> 32)
- *   y_i = dec_w . h_i + dec_b;  z_i = invdiag_i (r_i + sigma y_i)
+ *   y_i = dec_w . h_i + dec_b;  z_i = invdiag_i (r_i + theta sigma y_i)
+ * theta = 1 unless the correction would push z.r below half the Jacobi
+ * value r.(invdiag r); then theta is cut to hold z.r at that half.
  * h and the MLP inputs are BF16, the MLP runs on the tensor cores
  * (tcgen05, FP32 accumulation in tensor memory), aggregation in FP32.
  * Instances fall back to Jacobi (z = invdiag r, direction restart) when the
- * preconditioned direction breaks down (z.r <= 0) or the residual has not
- * decreased over `stall_window` iterations. */
+ * preconditioned direction breaks down (z.r <= 0 or non-finite), or at a
+ * check every `stall_window` iterations when r.r has not decreased since
+ * the last check or theta was cut in more than half of the window's
+ * iterations. */
 typedef struct {
   const float *node_lk;     /* [n] node input (log kappa); 0 on padding rows */
   const float *edge_feat;   /* [nslots][2] (w, len) per SELL slot            */
@@ -508,6 +512,7 @@ typedef struct {
   double sigma;      /* rms of r (GNN input scale)                          */
   double rr_mark;    /* r.r at the last stall check                         */
   double rz_jac;     /* r.(invdiag r) of the current residual               */
+  double theta;      /* weight of the network's correction in z (GNN mode)  */
   int32_t iters;     /* completed step() calls                              */
   int32_t done;      /* 0 running, 1 converged, 2 maxiter, 3 breakdown/NaN  */
   int32_t verified;  /* 1 = FP64 true residual <= tol                       */
@@ -517,7 +522,9 @@ typedef struct {
   int32_t refresh;   /* 1: next p-update restarts with p = invdiag r        */
   int32_t fallbacks; /* GNN -> Jacobi switches                              */
   int32_t nrows;     /* rows before padding                                 */
-  int32_t pad_;
+  int32_t gnn_iters; /* iteration of the last GNN -> Jacobi switch (0 none) */
+  int32_t clips;     /* iterations with theta < 1                           */
+  int32_t clips_mark;/* clips at the last stall check                       */
 } esr_bcg_inst;
 
 int64_t esr_bcg_workspace_bytes(int32_t ninst, int32_t nblocks,

@@ -79,17 +79,44 @@ def test_fcg_zero_output_is_jacobi_pcg():
         assert b["fallbacks"] == 0
 
 
-@pytest.mark.parametrize("precision", ["fp64", "df64"])
-def test_fcg_falls_back_to_jacobi(precision):
-    insts = p1_instances(3, 10, 40, seed=6)
-    eng = BatchedPCG(insts, jacobi=True, precision=precision, gnn=_sign_flip_weights())
-    res = eng.solve(rtol=1e-8)
-    for s, r in zip(insts, res):
-        assert r["status"] == "converged" and r["fallbacks"] >= 1 and r["mode"] == "jacobi"
-    for i, s in enumerate(insts):
+def _check_solutions(eng, insts, res):
+    for i, (s, r) in enumerate(zip(insts, res)):
+        assert r["status"] == "converged", r
         x = eng.solution(i).cpu().numpy()
         tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, s.b, x)
         assert tr <= 1e-8 * np.linalg.norm(s.b) * 1.0001
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_fcg_clips_a_negative_correction(precision):
+    """z = -r/Av from the network: theta holds z.r at half the Jacobi value
+    (z = invdiag r / 2), the solve goes on as scaled Jacobi."""
+    insts = p1_instances(3, 10, 40, seed=6)
+    eng = BatchedPCG(insts, jacobi=True, precision=precision, gnn=_sign_flip_weights(), stall_window=1 << 30)
+    res = eng.solve(rtol=1e-8)
+    assert all(r["clips"] >= 1 and r["fallbacks"] == 0 and r["mode"] == "gnn" for r in res)
+    _check_solutions(eng, insts, res)
+    # with the stall window on, a window of clipped iterations switches to Jacobi
+    eng = BatchedPCG(insts, jacobi=True, precision=precision, gnn=_sign_flip_weights(), stall_window=16)
+    res = eng.solve(rtol=1e-8)
+    for r in res:
+        if r["iters"] > 16:
+            assert r["fallbacks"] == 1 and r["fallback_iter"] == 16 and r["mode"] == "jacobi", r
+    _check_solutions(eng, insts, res)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_fcg_falls_back_to_jacobi_on_nonfinite_output(precision):
+    w = GnnWeights.zeros_output(1)
+    w.dec_b = float("nan")
+    insts = p1_instances(3, 10, 40, seed=6)
+    eng = BatchedPCG(insts, jacobi=True, precision=precision, gnn=w)
+    res = eng.solve(rtol=1e-8)
+    assert all(r["fallbacks"] == 1 and r["fallback_iter"] == 1 and r["mode"] == "jacobi" for r in res)
+    _check_solutions(eng, insts, res)
+    jac = BatchedPCG(insts, jacobi=True, precision=precision).solve(rtol=1e-8)
+    for a, b in zip(jac, res):
+        assert abs(a["iters"] - b["iters"]) <= max(3, a["iters"] // 50)
 
 
 def test_trained_weights_converge_if_present():
@@ -99,7 +126,4 @@ def test_trained_weights_converge_if_present():
     insts = p1_instances(6, 20, 80, seed=1)
     eng = BatchedPCG(insts, jacobi=True, precision="df64", gnn=GnnWeights.load())
     res = eng.solve(rtol=1e-8)
-    for i, (s, r) in enumerate(zip(insts, res)):
-        assert r["status"] == "converged"
-        x = eng.solution(i).cpu().numpy()
-        assert ocg.true_residual(s.row, s.col, s.Ae, s.Av, s.b, x) <= 1e-8 * np.linalg.norm(s.b) * 1.0001
+    _check_solutions(eng, insts, res)
