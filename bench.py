@@ -408,7 +408,7 @@ def bench_batched(args, world, rank, local):
     from easier_gb300.numeric.batched import BatchedPCG, p1_instances
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    prec = "fp64" if args.precision in ("native", "fp64") else "df64"
+    prec = "fp64" if args.precision == "fp64" else "df64"
     t0 = time.perf_counter()
     insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
     eng = BatchedPCG(insts, jacobi=True, precision=prec, device=dev, graph_iters=args.chunk)

@@ -302,6 +302,7 @@ int dispatch_delta(const esr_swe_mesh *m, const void *state, void *delta, cudaSt
 constexpr int kTileThreads = 1024;
 constexpr int kTileIters = 6;     // cells of level <= 3 per thread: <= 6 * 1024
 constexpr int kTileOwnIters = 4;  // tile cells per thread: <= 4 * 1024
+constexpr int kTileGroup = 2;     // cells whose geometry loads are issued together
 
 struct SlotsT {  // one tile's face slots, [3][n3]
   const int32_t *nb;
@@ -309,63 +310,106 @@ struct SlotsT {  // one tile's face slots, [3][n3]
   int n3, nL;
 };
 
+// geometry of one tile cell's three face slots
+struct CellGeom {
+  int32_t nb[3];
+  float al[3], sx[3], sy[3];
+  float area, inv_area;
+};
+
+// All 14 loads of a cell issue together (slot arrays have 3 x n3 entries,
+// so the unused alpha of a wall slot is still in bounds).
 template <bool EXACT>
-__device__ __forceinline__ void tile_delta(int j, const SlotsT &g, const float *hs, const float *us, const float *vs,
-                                           float &dh, float &du, float &dv) {
+__device__ __forceinline__ void load_geom(int j, const SlotsT &g, CellGeom &c) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    c.nb[k] = __ldg(g.nb + k * g.n3 + j);
+    c.al[k] = __ldg(g.al + k * g.n3 + j);
+    c.sx[k] = __ldg(g.sx + k * g.n3 + j);
+    c.sy[k] = __ldg(g.sy + k * g.n3 + j);
+  }
+  c.area = __ldg(g.area + j);
+  c.inv_area = EXACT ? 0.f : __ldg(g.inv_area + j);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, const float *hs, const float *us,
+                                           const float *vs, float &dh, float &du, float &dv) {
   const float oh = hs[j], ou = us[j], ov = vs[j];
   Acc3<float> acc{0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const int32_t q = __ldg(g.nb + k * g.n3 + j);
+    const int32_t q = c.nb[k];
     if (q >= 0) {
-      if (q >= g.nL) {  // corrupt layout: flag, never read outside the tile's list
+      if (q >= nL) {  // corrupt layout: flag, never read outside the tile's list
         esr::raise_status(ESR_DEV_IDX_RANGE);
         continue;
       }
-      add_face<float, EXACT>(acc, oh, ou, ov, hs[q], us[q], vs[q], __ldg(g.al + k * g.n3 + j),
-                             __ldg(g.sx + k * g.n3 + j), __ldg(g.sy + k * g.n3 + j));
+      add_face<float, EXACT>(acc, oh, ou, ov, hs[q], us[q], vs[q], c.al[k], c.sx[k], c.sy[k]);
     } else if (q == -1) {
-      add_wall<float, EXACT>(acc, oh, __ldg(g.sx + k * g.n3 + j), __ldg(g.sy + k * g.n3 + j));
+      add_wall<float, EXACT>(acc, oh, c.sx[k], c.sy[k]);
     }
   }
-  finish<float, EXACT>(acc, __ldg(g.area + j), EXACT ? 0.f : __ldg(g.inv_area + j), dh, du, dv);
+  finish<float, EXACT>(acc, c.area, c.inv_area, dh, du, dv);
 }
 
+template <int STAGE, bool EXACT>
+__device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &cg, int nL, const float *hs,
+                                          const float *us, const float *vs, const float *h0, const float *u0,
+                                          const float *v0, float *ho, float *uo, float *vo,
+                                          float (&acc)[kTileOwnIters][3], float c, float4 *sout, int64_t cell_off) {
+  using A = Ar<float, EXACT>;
+  float dh, du, dv;
+  tile_delta<EXACT>(j, cg, nL, hs, us, vs, dh, du, dv);
+  if (STAGE < 4) {
+    ho[j] = A::madd(c, dh, h0[j]);
+    uo[j] = A::madd(c, du, u0[j]);
+    vo[j] = A::madd(c, dv, v0[j]);
+    if (r < kTileOwnIters && j < n0) {
+      if (STAGE == 1) {
+        acc[r][0] = dh;
+        acc[r][1] = du;
+        acc[r][2] = dv;
+      } else {
+        acc[r][0] = A::add(acc[r][0], dh);
+        acc[r][1] = A::add(acc[r][1], du);
+        acc[r][2] = A::add(acc[r][2], dv);
+      }
+    }
+  } else if (r < kTileOwnIters) {
+    float4 o;
+    o.x = A::madd(c, A::add(acc[r][0], dh), h0[j]);
+    o.y = A::madd(c, A::add(acc[r][1], du), u0[j]);
+    o.z = A::madd(c, A::add(acc[r][2], dv), v0[j]);
+    o.w = 0.f;
+    sout[cell_off + j] = o;
+  }
+}
+
+// Cells j = tid + r * kTileThreads in groups of kTileGroup consecutive r:
+// the geometry of the whole group is requested before any of its cells is
+// computed, so the group's loads are in flight together (the kernel is
+// latency-bound on these L1/L2 loads otherwise).
 template <int STAGE, bool EXACT>
 __device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, const float *hs, const float *us,
                                            const float *vs, const float *h0, const float *u0, const float *v0,
                                            float *ho, float *uo, float *vo, float (&acc)[kTileOwnIters][3],
                                            float c, float4 *sout, int64_t cell_off) {
-  using A = Ar<float, EXACT>;
+  constexpr int kIters = STAGE == 4 ? kTileOwnIters : kTileIters;
 #pragma unroll
-  for (int r = 0; r < kTileIters; ++r) {
-    const int j = threadIdx.x + r * kTileThreads;
-    if (j < count) {
-      float dh, du, dv;
-      tile_delta<EXACT>(j, g, hs, us, vs, dh, du, dv);
-      if (STAGE < 4) {
-        ho[j] = A::madd(c, dh, h0[j]);
-        uo[j] = A::madd(c, du, u0[j]);
-        vo[j] = A::madd(c, dv, v0[j]);
-        if (r < kTileOwnIters && j < n0) {
-          if (STAGE == 1) {
-            acc[r][0] = dh;
-            acc[r][1] = du;
-            acc[r][2] = dv;
-          } else {
-            acc[r][0] = A::add(acc[r][0], dh);
-            acc[r][1] = A::add(acc[r][1], du);
-            acc[r][2] = A::add(acc[r][2], dv);
-          }
-        }
-      } else if (r < kTileOwnIters) {
-        float4 o;
-        o.x = A::madd(c, A::add(acc[r][0], dh), h0[j]);
-        o.y = A::madd(c, A::add(acc[r][1], du), u0[j]);
-        o.z = A::madd(c, A::add(acc[r][2], dv), v0[j]);
-        o.w = 0.f;
-        sout[cell_off + j] = o;
-      }
+  for (int r0 = 0; r0 < kIters; r0 += kTileGroup) {
+    CellGeom cg[kTileGroup];
+#pragma unroll
+    for (int u = 0; u < kTileGroup; ++u) {
+      const int j = threadIdx.x + (r0 + u) * kTileThreads;
+      if (r0 + u < kIters && j < count) load_geom<EXACT>(j, g, cg[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kTileGroup; ++u) {
+      const int j = threadIdx.x + (r0 + u) * kTileThreads;
+      if (r0 + u < kIters && j < count)
+        tile_cell<STAGE, EXACT>(r0 + u, j, n0, cg[u], g.nL, hs, us, vs, h0, u0, v0, ho, uo, vo, acc, c, sout,
+                                cell_off);
     }
   }
 }
