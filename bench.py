@@ -290,8 +290,12 @@ def bench_swe(args, world, rank, local):
                      "kernel": ("swe_tile_step_kernel (1 launch per step)" if eng.tiled else
                                 "swe_stage_kernel (4 launches per step; bytes and time per step / 4)"),
                      "algorithmic_bytes_per_launch": bytes_step / lps,
+                     "model": "per-step byte model of the unfused step: four delta passes (edge geometry, "
+                              "state, area, rowptr, delta out) and the stage combination through HBM; the "
+                              "fused kernel keeps the stage states on chip, so frac > 1 measures the fusion",
                      "touched_bytes_per_launch": touched / lps,
-                     "touched_frac": touched / (ms / args.steps / 1e3) / 1e9 / peak},
+                     "touched_frac": touched / (ms / args.steps / 1e3) / 1e9 / peak,
+                     "dram_frac": (traffic / (ms / args.steps / 1e3) / 1e9 / peak) if traffic else None},
         "precision": args.precision,
         "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
                    "within 1e-5 (FP32) / 1e-10 (FP64) relative of the reference FP64 run after 1,000 steps"),
