@@ -50,6 +50,11 @@ class CgScalars(Structure):
                 ("iters", c_int32), ("done", c_int32), ("maxiter", c_int32), ("replacements", c_int32)]
 
 
+class GmresScalars(Structure):
+    _fields_ = [("rnorm", c_double), ("bnorm", c_double), ("tol", c_double), ("jend", c_int32),
+                ("broken", c_int32), ("cycles", c_int32), ("pad_", c_int32)]
+
+
 class Gnn(Structure):
     _fields_ = [("node_lk", c_void_p), ("edge_feat", c_void_p), ("inst_rows", c_void_p), ("h0", c_void_p),
                 ("h1", c_void_p), ("enc_w", c_void_p), ("enc_b", c_void_p), ("layer_w", c_void_p),
@@ -122,9 +127,14 @@ _SIGS = {
     "esr_bcg_verify": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "esr_bcg_status": (c_int, [_P, c_int32, c_int32, POINTER(c_int32), POINTER(BcgInst), _P]),
     "esr_gnn_apply": (c_int, [POINTER(Batch), _P, _P, _P, _P]),
+    "esr_gmres_workspace_bytes": (c_int64, [c_int64, c_int32]),
+    "esr_gmres_init": (c_int, [POINTER(Sell), _P, c_double, c_double, _P, _P]),
+    "esr_gmres_residual": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P]),
+    "esr_gmres_cycle": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P, _P, c_int32, _P, _P]),
+    "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 
 def library_path() -> Path:

@@ -136,9 +136,48 @@ class GMRES(esr.Module):
         self.y = esr.Tensor(torch.zeros((restart, 1), dtype=x.dtype, device=x.device), mode="replicate")
         self.update_x = nn.ModuleList([UpdateX(self.x, self.V, self.M, self.y, i) for i in range(1, restart + 1)])
 
+    # ------------------------------------------------------------ fused --
+    def fusable(self) -> bool:
+        from ..linsys import Linsys
+        from ..preconditioner.jacobi import Jacobi
+        if not isinstance(self.A, Linsys) or not (self.M is _identity or isinstance(self.M, Jacobi)):
+            return False
+        A = self.A
+        ok = (A.selector.easier_index_status == "rewritten" and A.reducer.easier_index_status == "rewritten"
+              and self.x.easier_data_ready and self.b.easier_data_ready)
+        return bool(ok) and self.x.is_cuda and self.x.dtype in (torch.float32, torch.float64) \
+            and A.Ae.dtype == self.x.dtype and A.Av.dtype == self.x.dtype and self.x.dim() == 1 \
+            and self.x.elempart is None and 1 <= self.restart <= 64
+
+    def _fused_solver(self):
+        from ..preconditioner.jacobi import Jacobi
+        from ..sparse import FusedGMRES, SellMatrix
+        A = self.A
+        key = (A.Ae.data.data_ptr(), A.Ae._version, A.Av.data.data_ptr(), A.Av._version, self.restart)
+        if getattr(self, "_fused", None) is None or self._fused_key != key:
+            self._fused = FusedGMRES(SellMatrix.from_linsys(A), self.restart, jacobi=isinstance(self.M, Jacobi))
+            self._fused_key = key
+        return self._fused
+
     def solve(self, rtol: float = 1e-5, atol: Optional[float] = None, maxiter: Optional[int] = None,
-              debug_iter: Optional[int] = None) -> Dict[str, Any]:
+              debug_iter: Optional[int] = None, *, fused: Optional[bool] = None) -> Dict[str, Any]:
+        """Solve to ``rnorm <= max(rtol*||b||, atol)`` (gmres.py:222-266).
+        With a compiled ``Linsys`` and ``M`` None or ``Jacobi`` every restart
+        cycle runs as one CUDA graph of fused kernels (``fused=False``
+        forces the per-op modules)."""
         name = self.__class__.__name__
+        use_fused = self.fusable() if fused is None else fused
+        if use_fused:
+            eng = self._fused_solver()
+
+            def log(it, rn):
+                if debug_iter is not None and it % debug_iter == 0:
+                    logger.info(f"{name} residual {rn} at the {it}-th iteration")
+            s, iters = eng.solve(self.b.data, self.x.data, self.r.data, rtol, atol, maxiter, log)
+            self.rnorm.data.fill_(s.rnorm)
+            self.bnorm.data.fill_(s.bnorm)
+            logger.info(f"{name} solver completed with residual {s.rnorm} at the {iters}-th iteration")
+            return {"residual": float(s.rnorm), "iters": iters}
         self.init()
         rtol_t = rtol * self.bnorm
         tol = torch.maximum(rtol_t, torch.as_tensor(atol, dtype=rtol_t.dtype, device=rtol_t.device)) \

@@ -226,3 +226,77 @@ class MixedPCG:
             self.kernel_launches += 3 * self.chunk + 1
             s = self.scalars()
         return s
+
+
+class FusedGMRES:
+    """Restarted GMRES on a SELL matrix with M = Jacobi or identity
+    (gmres.py algorithm): one CUDA graph per restart cycle, one 64-byte read
+    of the device scalars per cycle for the host's stopping test."""
+
+    def __init__(self, A: SellMatrix, restart: int, jacobi: bool = False, use_graph: bool = True):
+        self.A = A
+        self.n = A.n
+        self.dev = A.device
+        self.dtype = A.dtype
+        self.restart = int(restart)
+        self.invdiag = (1.0 / A.diag).contiguous() if jacobi else None
+        nbytes = int(_lib.lib().esr_gmres_workspace_bytes(self.n, self.restart))
+        if nbytes < 0:
+            raise ValueError("fused GMRES supports restart <= 64")
+        self.ws = torch.zeros(nbytes, dtype=torch.uint8, device=self.dev)
+        self.V = torch.empty((self.restart, self.n), dtype=self.dtype, device=self.dev)
+        self.w2 = torch.empty((2, self.n), dtype=self.dtype, device=self.dev)
+        self.use_graph = use_graph
+        self._graphs = {}
+        self.kernel_launches = 0
+
+    def launches_per_cycle(self) -> int:
+        R = self.restart
+        return 1 + R + R * (R + 1) // 2 + 3
+
+    def scalars(self) -> _lib.GmresScalars:
+        out = _lib.GmresScalars()
+        _lib.call("esr_gmres_read", _lib.ptr(self.ws), ctypes.byref(out), _lib.stream_handle(self.dev))
+        return out
+
+    def _cycle_call(self, b, x, r):
+        _lib.call("esr_gmres_cycle", ctypes.byref(self.A.desc), _lib.ptr(self.invdiag), _lib.ptr(b), _lib.ptr(x),
+                  _lib.ptr(r), _lib.ptr(self.V), _lib.ptr(self.w2), self.restart, _lib.ptr(self.ws),
+                  _lib.stream_handle(self.dev))
+
+    def _cycle(self, b, x, r):
+        self.kernel_launches += self.launches_per_cycle()
+        if not self.use_graph:
+            self._cycle_call(b, x, r)
+            return
+        key = (b.data_ptr(), x.data_ptr(), r.data_ptr())
+        g = self._graphs.get(key)
+        if g is None:
+            s = torch.cuda.Stream(self.dev)
+            s.wait_stream(torch.cuda.current_stream(self.dev))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self._cycle_call(b, x, r)
+            torch.cuda.current_stream(self.dev).wait_stream(s)
+            self._graphs[key] = g
+        g.replay()
+
+    def solve(self, b, x, r, rtol: float, atol: Optional[float], maxiter: Optional[int], log=None):
+        """The reference's loop (gmres.py:229-266): residual, stopping test,
+        one restart cycle per iteration.  Returns (scalars, iters)."""
+        st = _lib.stream_handle(self.dev)
+        _lib.call("esr_gmres_init", ctypes.byref(self.A.desc), _lib.ptr(b), float(rtol),
+                  float(atol) if atol else 0.0, _lib.ptr(self.ws), st)
+        _lib.call("esr_gmres_residual", ctypes.byref(self.A.desc), _lib.ptr(b), _lib.ptr(x), _lib.ptr(r),
+                  _lib.ptr(self.ws), st)
+        self.kernel_launches += 2
+        iters = 0
+        while True:
+            s = self.scalars()
+            if log is not None:
+                log(iters, s.rnorm)
+            if (s.rnorm == s.rnorm and s.rnorm <= s.tol) or (maxiter is not None and iters >= maxiter):
+                return s, iters
+            iters += 1
+            self._cycle(b, x, r)

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 4
+#define ESR_GB300_ABI_VERSION 5
 
 /* element types */
 enum {
@@ -428,6 +428,46 @@ int esr_convert(int dtype_in, const void *in, int dtype_out, void *out,
  * correction of mixed-precision CG (no reference counterpart). */
 int esr_axpy_f64(double *x, int dtype_d, const void *d, double scale,
                  int64_t n, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Fused restarted GMRES (easier/numeric/solver/gmres.py:139-266) on a
+ * SELL-32 Linsys, F32 or F64, M = Jacobi (invdiag) or identity (NULL).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  double rnorm;    /* ||b - A x|| after the last residual evaluation        */
+  double bnorm;
+  double tol;      /* max(rtol * bnorm, atol)                              */
+  int32_t jend;    /* Arnoldi columns of the last cycle                    */
+  int32_t broken;  /* the last cycle stopped on H[j+1][j] < 1e-15          */
+  int32_t cycles;  /* restart cycles run since esr_gmres_init             */
+  int32_t pad_;
+} esr_gmres_scalars;
+
+/* Scratch bytes (restart <= 64). */
+int64_t esr_gmres_workspace_bytes(int64_t n, int32_t restart);
+
+/* bnorm = ||b||, tol = max(rtol * bnorm, atol) (gmres.py:232-234);
+ * zeroes the workspace. */
+int esr_gmres_init(const esr_sell *A, const void *b, double rtol, double atol,
+                   void *workspace, void *stream);
+
+/* r = b - A x, rnorm = ||r|| (UpdateRnorm, gmres.py:21-24). */
+int esr_gmres_residual(const esr_sell *A, const void *b, const void *x, void *r,
+                       void *workspace, void *stream);
+
+/* One restart cycle (gmres.py:245-261): V_0 = r / rnorm, `restart` Arnoldi
+ * steps with modified Gram-Schmidt in the reference's order (stopping early
+ * on H[j+1][j] < 1e-15), the Hessenberg least squares on the device (Givens
+ * rotations; the reference's clamped SVD gives the same y for a full-rank
+ * H), x += M (V y), then the residual for the next stopping test.  V is
+ * [restart][n] (column-contiguous), w2 is [2][n] scratch.  A fixed launch
+ * sequence: capturable in a CUDA graph. */
+int esr_gmres_cycle(const esr_sell *A, const void *invdiag, const void *b,
+                    void *x, void *r, void *V, void *w2, int32_t restart,
+                    void *workspace, void *stream);
+
+/* Copy the scalars to host memory (synchronises `stream`). */
+int esr_gmres_read(const void *workspace, esr_gmres_scalars *out, void *stream);
 
 /* ------------------------------------------------------------------------
  * Batched (P)CG: `ninst` independent Linsys instances packed as one

@@ -126,12 +126,44 @@ def test_maxiter_and_status():
     assert info["iters"] == 5 and info["status"] == "maxiter"
 
 
-def test_gmres_per_op_path_vs_reference(golden):
+@pytest.mark.parametrize("fused", [False, True])
+def test_gmres_vs_reference(golden, fused):
     g = golden("poisson_fv_n10_solve.npz")
     eqn = workloads.make_poisson_fv(10)
     sol = GMRES(eqn.A, eqn.b, eqn.x)
     [eqn, sol] = esr.compile([eqn, sol], "cuda")
-    info = sol.solve(rtol=1e-8, maxiter=2000)
+    assert sol.fusable()
+    info = sol.solve(rtol=1e-8, maxiter=2000, fused=fused)
     assert abs(info["iters"] - int(g["gmres_iters"])) <= 2
     x = eqn.x.collect().cpu().numpy()
     assert np.linalg.norm(x - g["gmres_x"]) <= 1e-6 * np.linalg.norm(g["gmres_x"])
+
+
+def test_fused_gmres_matches_per_op_path():
+    """Fused restart cycles (CUDA graph) vs the reference's modules run
+    per-op on the GB300 kernels: same iteration count, same solution to
+    the solve tolerance; Jacobi and identity M; a short restart."""
+    for M_jacobi, restart in ((True, 20), (False, 7)):
+        eqn = workloads.P1Poisson(20, rhs_seed=5)
+        sol = GMRES(eqn.A, eqn.b, eqn.x, M=Jacobi(eqn.A) if M_jacobi else None, restart=restart)
+        [eqn, sol] = esr.compile([eqn, sol], "cuda")
+        assert sol.fusable()
+        info_f = sol.solve(rtol=1e-8, maxiter=500)
+        x_f = eqn.x.collect().clone()
+        eqn.x.data.zero_()
+        info_p = sol.solve(rtol=1e-8, maxiter=500, fused=False)
+        x_p = eqn.x.collect()
+        assert abs(info_f["iters"] - info_p["iters"]) <= 1, (info_f, info_p)
+        assert torch.allclose(x_f, x_p, rtol=1e-6, atol=1e-9)
+        b = eqn.b.collect().cpu().numpy()
+        s = mesh.p1_system(20)
+        tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, b, x_f.cpu().numpy())
+        assert tr <= 1e-8 * np.linalg.norm(b) * 1.0001
+
+
+def test_fused_gmres_maxiter():
+    eqn = workloads.P1Poisson(40, rhs_seed=1)
+    sol = GMRES(eqn.A, eqn.b, eqn.x, restart=5)
+    [eqn, sol] = esr.compile([eqn, sol], "cuda")
+    info = sol.solve(rtol=1e-12, maxiter=3)
+    assert info["iters"] == 3 and info["residual"] > 0
