@@ -127,6 +127,7 @@ _SIGS = {
     "esr_bcg_verify": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "esr_bcg_status": (c_int, [_P, c_int32, c_int32, POINTER(c_int32), POINTER(BcgInst), _P]),
     "esr_gnn_apply": (c_int, [POINTER(Batch), _P, _P, _P, _P]),
+    "esr_wait_selftest": (c_int, [c_int32, _P, _P]),
     "esr_gmres_workspace_bytes": (c_int64, [c_int64, c_int32]),
     "esr_gmres_init": (c_int, [POINTER(Sell), _P, c_double, c_double, _P, _P]),
     "esr_gmres_residual": (c_int, [POINTER(Sell), _P, _P, _P, _P, _P]),

@@ -112,6 +112,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
   return ok != 0;
 }
 
+// Bounded wait for phase `parity` of an mbarrier: at most `limit` polls
+// (each try_wait may suspend briefly); false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *mbar, uint32_t parity, int limit) {
+  bool ok = false;
+  for (int tries = 0; tries < limit && !ok; ++tries) ok = mbar_try_wait(mbar, parity);
+  return ok;
+}
+
 // 8 consecutive FP32 accumulator columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
@@ -279,9 +287,7 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
           mma_bf16(tmem, mma_desc(ua + k * 2 * kCoreBytes), mma_desc(wa + k * 2 * kCoreBytes), k > 0 ? 1u : 0u);
         mma_commit(&s_mbar);
       }
-      bool ok = false;
-      for (int tries = 0; tries < kWaitLimit && !ok; ++tries) ok = mbar_try_wait(&s_mbar, phase);
-      if (!ok) s_err = 1;
+      if (!mbar_wait_bounded(&s_mbar, phase, kWaitLimit)) s_err = 1;
       phase ^= 1u;
       tc_fence_after();
       __syncthreads();
@@ -385,9 +391,39 @@ int launch_layers(const esr_batch *B, const void *r, const void *q, void *z, voi
   return ESR_OK;
 }
 
+// Self-test of the bounded wait: allocates tensor memory like the layer
+// kernel, waits on an mbarrier that nothing arrives on, and must give up,
+// raise ESR_DEV_WAIT_TIMEOUT, free the tensor memory and return.
+__global__ void __launch_bounds__(32) gnn_wait_selftest_kernel(int limit, int *gave_up) {
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  if (threadIdx.x == 0) mbar_init(&s_mbar);
+  tmem_alloc(&s_tmem, kTmemCols);
+  tmem_relinquish();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const bool ok = mbar_wait_bounded(&s_mbar, 0u, limit);
+  __syncthreads();
+  tc_fence_after();
+  tmem_dealloc(s_tmem, kTmemCols);
+  if (threadIdx.x == 0) {
+    *gave_up = ok ? 0 : 1;
+    if (!ok) esr::raise_status(ESR_DEV_WAIT_TIMEOUT);
+  }
+}
+
 }  // namespace
 
 ESR_DEFINE_STATUS_READER(esr_status_gnn)
+
+extern "C" int esr_wait_selftest(int32_t limit_polls, int32_t *gave_up_dev, void *stream) {
+  if (limit_polls <= 0 || limit_polls > kWaitLimit || !gave_up_dev)
+    return esr::fail(ESR_ERR_ARG, "esr_wait_selftest: limit in [1, 2^22] and a device flag");
+  gnn_wait_selftest_kernel<<<1, 32, 0, esr::as_stream(stream)>>>(limit_polls, gave_up_dev);
+  ESR_LAUNCH_CHECK("esr_wait_selftest");
+  return ESR_OK;
+}
 
 namespace esr {
 int gnn_layers(const esr_batch *B, const void *r, const void *q, void *z, void *workspace, cudaStream_t s) {

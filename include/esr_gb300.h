@@ -598,6 +598,13 @@ int esr_bcg_verify(const esr_batch *B, const double *b64, void *x, double *x64,
 int esr_gnn_apply(const esr_batch *B, const void *r, void *z, void *workspace,
                   void *stream);
 
+/* Self-test of the bounded device wait used by the GNN kernels: one warp
+ * allocates tensor memory, waits at most `limit_polls` polls on an mbarrier
+ * that nothing arrives on, frees the tensor memory, writes 1 to
+ * *gave_up_dev and raises ESR_DEV_WAIT_TIMEOUT.  The context stays usable.
+ * Test hook (no reference counterpart). */
+int esr_wait_selftest(int32_t limit_polls, int32_t *gave_up_dev, void *stream);
+
 /* Running-instance count and (if inst_out) the per-instance scalars, to
  * host memory; synchronises `stream`. */
 int esr_bcg_status(const void *workspace, int32_t ninst, int32_t nchunks,

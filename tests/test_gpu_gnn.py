@@ -127,3 +127,19 @@ def test_trained_weights_converge_if_present():
     eng = BatchedPCG(insts, jacobi=True, precision="df64", gnn=GnnWeights.load())
     res = eng.solve(rtol=1e-8)
     _check_solutions(eng, insts, res)
+
+
+def test_bounded_wait_gives_up_and_context_survives():
+    """The GNN kernels' mbarrier wait is bounded: a wait that nothing
+    completes returns with ESR_DEV_WAIT_TIMEOUT; later work still runs."""
+    from easier_gb300 import _lib, ops
+    ops.device_status(clear=True)
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("esr_wait_selftest", 1 << 12, _lib.ptr(flag), _lib.stream_handle())
+    assert int(flag.item()) == 1
+    assert ops.device_status(clear=True) & _lib.DEV_WAIT_TIMEOUT
+    # the context is intact: a batched solve right after
+    insts = p1_instances(2, 8, 12, seed=2)
+    res = BatchedPCG(insts, jacobi=True, precision="fp64").solve(rtol=1e-8)
+    assert all(r["status"] == "converged" for r in res)
+    assert ops.device_status(clear=True) == 0
