@@ -141,11 +141,11 @@ def compile(modules: List[_m.Module], backend: Literal["torch", "cpu", "cuda", "
         raise EasierJitException(
             "easier_gb300 implements the CUDA backend only (backend='cuda'); the CPU backends are the"
             " reference package's")
-    if not torch.cuda.is_available():
-        raise EasierJitException("backend='cuda' needs a CUDA device")
     if _world_size() > 1:
         raise EasierJitException(
             "easier_gb300 runs at world size 1 (one GPU per process, independent replicas)")
+    if not torch.cuda.is_available():
+        raise EasierJitException("backend='cuda' needs a CUDA device")
     device = torch.device("cuda", torch.cuda.current_device())
     from . import _lib
     _lib.lib()  # fail now, loudly, if the native library is unusable
