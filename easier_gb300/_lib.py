@@ -34,8 +34,8 @@ class SweTiles(Structure):
     _fields_ = [("nc", c_int64), ("ntiles", c_int32), ("dtype", c_int32), ("max_local", c_int32),
                 ("max_l3", c_int32), ("max_own", c_int32), ("pad_", c_int32),
                 ("meta", c_void_p), ("off3", c_void_p), ("offh", c_void_p), ("halo", c_void_p),
-                ("lnbr", c_void_p), ("sx", c_void_p), ("sy", c_void_p), ("alpha", c_void_p), ("area", c_void_p),
-                ("inv_area", c_void_p), ("exact", c_int32), ("pad2_", c_int32)]
+                ("slots", c_void_p), ("area", c_void_p), ("inv_area", c_void_p), ("exact", c_int32),
+                ("pad2_", c_int32)]
 
 
 class Sell(Structure):
@@ -135,7 +135,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 
 def library_path() -> Path:

@@ -304,9 +304,9 @@ constexpr int kTileIters = 6;     // cells of level <= 3 per thread: <= 6 * 1024
 constexpr int kTileOwnIters = 4;  // tile cells per thread: <= 4 * 1024
 constexpr int kTileGroup = 2;     // cells whose geometry loads are issued together
 
-struct SlotsT {  // one tile's face slots, [3][n3]
-  const int32_t *nb;
-  const float *sx, *sy, *al, *area, *inv_area;
+struct SlotsT {  // one tile's face slots, [3][n3] records {sx, sy, alpha, lnbr}
+  const float4 *slot;
+  const float *area, *inv_area;
   int n3, nL;
 };
 
@@ -317,16 +317,17 @@ struct CellGeom {
   float area, inv_area;
 };
 
-// All 14 loads of a cell issue together (slot arrays have 3 x n3 entries,
-// so the unused alpha of a wall slot is still in bounds).
+// The cell's geometry: three 16-byte face records and its area, all
+// loads issued together.
 template <bool EXACT>
 __device__ __forceinline__ void load_geom(int j, const SlotsT &g, CellGeom &c) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    c.nb[k] = __ldg(g.nb + k * g.n3 + j);
-    c.al[k] = __ldg(g.al + k * g.n3 + j);
-    c.sx[k] = __ldg(g.sx + k * g.n3 + j);
-    c.sy[k] = __ldg(g.sy + k * g.n3 + j);
+    const float4 f = __ldg(g.slot + k * g.n3 + j);
+    c.sx[k] = f.x;
+    c.sy[k] = f.y;
+    c.al[k] = f.z;
+    c.nb[k] = __float_as_int(f.w);
   }
   c.area = __ldg(g.area + j);
   c.inv_area = EXACT ? 0.f : __ldg(g.inv_area + j);
@@ -418,8 +419,7 @@ template <bool EXACT>
 __global__ void __launch_bounds__(kTileThreads, 1)
 swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
-                     const int32_t *__restrict__ lnbr, const float *__restrict__ gsx, const float *__restrict__ gsy,
-                     const float *__restrict__ gal, const float *__restrict__ garea,
+                     const float4 *__restrict__ gslot, const float *__restrict__ garea,
                      const float *__restrict__ ginv_area, const float4 *__restrict__ sin,
                      float4 *__restrict__ sout, int64_t nc, int max_local, int max_l3, float c1, float c3,
                      float c4) {
@@ -447,8 +447,7 @@ swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   }
   __syncthreads();
   const int64_t o3 = off3[t];
-  const SlotsT g{lnbr + 3 * o3, gsx + 3 * o3, gsy + 3 * o3, gal + 3 * o3, garea + o3,
-                 EXACT ? nullptr : ginv_area + o3, n3, nL};
+  const SlotsT g{gslot + 3 * o3, garea + o3, EXACT ? nullptr : ginv_area + o3, n3, nL};
   float acc[kTileOwnIters][3];
 #pragma unroll
   for (int r = 0; r < kTileOwnIters; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.f;
@@ -475,8 +474,8 @@ int check_tiles(const esr_swe_tiles *T) {
     return esr::fail(ESR_ERR_UNSUPPORTED, "a tile plus 3 halo rings has more than 6144 cells");
   if (T->max_local < T->max_l3 || T->max_l3 < T->max_own) return esr::fail(ESR_ERR_ARG, "inconsistent tile maxima");
   if (tile_smem_bytes(T) > 227 * 1024) return esr::fail(ESR_ERR_UNSUPPORTED, "tile needs more than 227 KB shared memory");
-  if (!T->meta || !T->off3 || !T->offh || !T->lnbr || !T->sx || !T->sy || !T->alpha || !T->area)
-    return esr::fail(ESR_ERR_ARG, "null tile array");
+  if (!T->meta || !T->off3 || !T->offh || !T->slots || !T->area) return esr::fail(ESR_ERR_ARG, "null tile array");
+  if (reinterpret_cast<uintptr_t>(T->slots) % 16 != 0) return esr::fail(ESR_ERR_ARG, "slots must be 16-byte aligned");
   if (!T->exact && !T->inv_area) return esr::fail(ESR_ERR_ARG, "fast arithmetic needs inv_area");
   return ESR_OK;
 }
@@ -491,10 +490,9 @@ int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_
   float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
   for (int64_t k = 0; k < steps; ++k) {
     swe_tile_step_kernel<EXACT><<<tiles->ntiles, kTileThreads, smem, s>>>(
-        tiles->meta, tiles->off3, tiles->offh, tiles->halo, tiles->lnbr, (const float *)tiles->sx,
-        (const float *)tiles->sy, (const float *)tiles->alpha, (const float *)tiles->area,
-        (const float *)tiles->inv_area, buf[k & 1], buf[(k + 1) & 1], tiles->nc, tiles->max_local, tiles->max_l3,
-        c1, c3, c4);
+        tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots,
+        (const float *)tiles->area, (const float *)tiles->inv_area, buf[k & 1], buf[(k + 1) & 1], tiles->nc,
+        tiles->max_local, tiles->max_l3, c1, c3, c4);
   }
   ESR_LAUNCH_CHECK("esr_swe_tile_step");
   return ESR_OK;

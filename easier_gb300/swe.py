@@ -197,17 +197,18 @@ class SweEngine:
                                   _lib.ptr(self.sx), _lib.ptr(self.sy), _lib.ptr(self.alpha), _lib.ptr(self.area),
                                   _lib.ptr(self.inv_area), exact, 0)
         if self.tiled:
-            self.t_sx = self.sx.reshape(-1)[self.tile_gsrc].contiguous()
-            self.t_sy = self.sy.reshape(-1)[self.tile_gsrc].contiguous()
-            self.t_alpha = self.alpha.reshape(-1)[self.tile_gsrc].contiguous()
+            src = self.tile_gsrc
+            # one 16-byte record per tile face slot: sx, sy, alpha, lnbr bits
+            self.t_slots = torch.stack([self.sx.reshape(-1)[src], self.sy.reshape(-1)[src],
+                                        self.alpha.reshape(-1)[src], self.tile_lnbr.view(torch.float32)],
+                                       dim=1).contiguous()
             self.t_area = self.area[self.tile_area_src].contiguous()
             self.t_inv_area = self.inv_area[self.tile_area_src].contiguous()
             st = self.tile_stats
             self._tiles = _lib.SweTiles(self.nc, self.ntiles, _lib.F32, st["max_local"], st["max_l3"],
                                         st["max_own"], 0, _lib.ptr(self.tile_meta), _lib.ptr(self.tile_off3),
                                         _lib.ptr(self.tile_offh), _lib.ptr(self.tile_halo),
-                                        _lib.ptr(self.tile_lnbr), _lib.ptr(self.t_sx), _lib.ptr(self.t_sy),
-                                        _lib.ptr(self.t_alpha), _lib.ptr(self.t_area), _lib.ptr(self.t_inv_area),
+                                        _lib.ptr(self.t_slots), _lib.ptr(self.t_area), _lib.ptr(self.t_inv_area),
                                         exact, 0)
 
     def set_precision(self, precision: str) -> None:

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 5
+#define ESR_GB300_ABI_VERSION 6
 
 /* element types */
 enum {
@@ -262,8 +262,10 @@ int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *delta,
  * levels <= 2, j < n3 levels <= 3, j < nL all.  Per tile:
  *   meta[8t..8t+5] = cell_off, n0, n1, n2, n3, nL
  *   halo[offh[t] + j - n0] = global cell of local j >= n0
- *   per local cell j < n3 and slot k: lnbr/sx/sy/alpha[3*off3[t] + k*n3 + j]
- *   (lnbr = local index of the neighbour, -1 wall, -2 empty), area[off3[t] + j].
+ *   per local cell j < n3 and slot k: slots[3*off3[t] + k*n3 + j] = one
+ *   16-byte record {float sx, float sy, float alpha, int32 lnbr} (lnbr =
+ *   local index of the neighbour, -1 wall, -2 empty; one vector load per
+ *   face), area[off3[t] + j].
  * Limits: n0 <= 4096, n3 <= 6144, 12*nL + 24*n3 bytes <= 227 KB. */
 typedef struct {
   int64_t nc;
@@ -277,10 +279,7 @@ typedef struct {
   const int64_t *off3;
   const int64_t *offh;
   const int32_t *halo;
-  const int32_t *lnbr;
-  const void *sx;
-  const void *sy;
-  const void *alpha;
+  const void *slots;  /* 16-byte aligned face-slot records, see above */
   const void *area;
   const void *inv_area; /* [sum(n3)], used when exact == 0 */
   int32_t exact;        /* as in esr_swe_mesh */
