@@ -122,7 +122,7 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
 
 // ---- step part 1: q = A p; p.q; alpha
 template <class P>
-__global__ void __launch_bounds__(kBThreads)
+__global__ void __launch_bounds__(kBThreads, 4)
 bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P::V *__restrict__ diag,
                 const typename P::V *__restrict__ p, typename P::V *__restrict__ q, BcgLayout L) {
   using V = typename P::V;
@@ -133,6 +133,7 @@ bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     if (L.inst[inst].done) continue;
     typename P::Acc pq;
     const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
       const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
       const V pi = p[i];
@@ -172,6 +173,7 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
     const V av = P::of(ad), nav = P::of(-ad);
     typename P::Acc rr, rz;
     const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
       const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
       x[i] = P::fma(av, p[i], x[i]);
@@ -244,6 +246,7 @@ bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, const typename 
     const bool blend = L.inst[inst].mode == kModeGnn && theta != 1.0;
     const V th = P::of(theta), omth = P::of(1.0 - theta);
     const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
       const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
       if (refresh) {
