@@ -103,6 +103,10 @@ class CG(esr.Module):
             and self.x.elempart is None
 
     def _fused_solver(self, precision: str):
+        """The engine for `precision`: FP64 systems ('native' and 'df64') run
+        on the batched lockstep engine as a batch of one (autotuned work
+        shape, FP64-verified result); 'native' FP32 systems on FusedPCG;
+        'mixed' on MixedPCG."""
         from ..sparse import FusedPCG, MixedPCG, SellMatrix
         A = self.A
         key = (precision, A.Ae.data.data_ptr(), A.Ae._version, A.Av.data.data_ptr(), A.Av._version)
@@ -112,12 +116,13 @@ class CG(esr.Module):
                 raise ValueError(f"precision='{precision}' needs an FP64 system")
             if precision == "mixed":
                 self._fused = MixedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
-            elif precision == "df64":
+            elif precision == "df64" or A.Av.dtype == torch.float64:
                 from ..batched import BatchedPCG, LinsysInstance
                 n = A.Av.shape[0]
                 inst = LinsysInstance(n, A.reducer.idx.detach().cpu().numpy(), A.selector.idx.detach().cpu().numpy(),
                                       A.Ae.data, A.Av.data, self.b.data)
-                self._fused = BatchedPCG([inst], jacobi=jacobi, precision="df64", device=self.x.device)
+                self._fused = BatchedPCG([inst], jacobi=jacobi, precision="df64" if precision == "df64" else "fp64",
+                                         device=self.x.device)
                 self._fused.autotune()
             else:
                 self._fused = FusedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
@@ -164,9 +169,10 @@ class CG(esr.Module):
 
     def _solve_fused(self, rtol, atol, maxiter, precision) -> Dict[str, Any]:
         name = self.__class__.__name__
+        from ..batched import BatchedPCG
         eng = self._fused_solver(precision)
         x, b = self.x.data, self.b.data
-        if precision == "df64":
+        if isinstance(eng, BatchedPCG):
             eng.load_instance(0, b=b, x0=x)
             [res] = eng.solve(rtol, atol, maxiter)
             x.copy_(eng.solution(0).to(x.dtype))
@@ -174,7 +180,7 @@ class CG(esr.Module):
             self.rnorm.data.fill_(res["residual"])
             self.bnorm.data.fill_(res["bnorm"])
             info = {"residual": res["residual"], "iters": res["iters"], "true_residual": rn,
-                    "restarts": res["restarts"], "precision": "df64", "status": res["status"]}
+                    "restarts": res["restarts"], "precision": precision, "status": res["status"]}
         elif precision == "mixed":
             s = eng.solve(b, x, self.r.data, self.z.data, self.p.data, rtol, atol, maxiter)
             rn = float(s.true_rr) ** 0.5
