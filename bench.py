@@ -423,9 +423,19 @@ def bench_batched(args, world, rank, local):
     tune_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream(dev)
     x_start = torch.zeros_like(eng.b64)
+    maxiter = 100000  # bounds the device-side loop of the one-launch graph
+
+    def one_solve():
+        # the whole batch solve is ONE CUDA graph launch (init, device-side
+        # loop of iteration bodies with FP64 verification)
+        if args.polled:
+            eng.run(1e-8)
+        else:
+            eng.solve_graph(1e-8, maxiter=maxiter)
+
     for _ in range(args.warmup):
         eng.load_packed(x0=x_start)
-        eng.run(1e-8)
+        one_solve()
     torch.cuda.synchronize(dev)
     launches0 = eng.kernel_launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -435,13 +445,18 @@ def bench_batched(args, world, rank, local):
         e0.record(stream)
         for _ in range(args.steps):
             eng.load_packed(x0=x_start)
-            eng.run(1e-8)
+            one_solve()
         e1.record(stream)
         torch.cuda.synchronize(dev)
         _barrier(world)
     ms = _max_over_ranks(world, e0.elapsed_time(e1))
-    launches = eng.kernel_launches - launches0
     res = [eng._info(s) for s in eng.instances()]
+    if args.polled:
+        launches = eng.kernel_launches - launches0
+    else:  # kernels the device-side loop ran: init, then per body compaction, k iterations, verification
+        kk = eng.graph_iters
+        bodies = -(-(max(r["iters"] for r in res) + 1) // kk)
+        launches = args.steps * (1 + bodies * (1 + 3 * kk + 4 + 1))
     bad = [i for i, r in enumerate(res) if r["status"] != "converged" or not r["true_residual"] <= 1e-8 * r["bnorm"]
            * 1.0001]
     if bad:
@@ -463,7 +478,7 @@ def bench_batched(args, world, rank, local):
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
         eng.load_packed(b64=b_host.to(dev, non_blocking=True), x0=x_start)
-        eng.run(1e-8)
+        one_solve()
         x_host.copy_(eng.solution(), non_blocking=True)
     torch.cuda.synchronize(dev)
     e2e_sec = (time.perf_counter() - t0) / e2e_steps
@@ -479,6 +494,8 @@ def bench_batched(args, world, rank, local):
                    "iterations_max": max(iters), "iterations_mean": float(np.mean(iters)),
                    "restarts": int(sum(r["restarts"] for r in res)), "precision": prec,
                    "graph_iters": eng.graph_iters, "tiles_per_chunk": eng.tiles_per_chunk, "grid": eng.grid,
+                   "launch": ("host-polled CUDA graphs of graph_iters iterations" if args.polled else
+                              "one CUDA graph launch per batch solve (device-side while loop)"),
                    "autotune": None if tuning is None else
                    {"s": tune_s, "ms_per_iter_all_running": tuning["ms_per_iter"],
                     "candidates": len(tuning["table"])},
@@ -644,6 +661,7 @@ def main():
     ap.add_argument("--seed", type=int, default=None, help="batched: instance seed (gnn: held-out seed 1)")
     ap.add_argument("--chunk", type=int, default=32, help="batched: iterations per CUDA graph")
     ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default work shape")
+    ap.add_argument("--polled", action="store_true", help="batched: host-polled graphs instead of one launch")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
     ap.add_argument("--dt", type=float, default=None)

@@ -127,6 +127,10 @@ _SIGS = {
     "esr_bcg_verify": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "esr_bcg_status": (c_int, [_P, c_int32, c_int32, POINTER(c_int32), POINTER(BcgInst), _P]),
     "esr_gnn_apply": (c_int, [POINTER(Batch), _P, _P, _P, _P]),
+    "esr_bcg_graph_create": (c_int, [POINTER(Batch), _P, _P, _P, _P, _P, _P, _P, _P, _P, c_double, c_double, c_int32,
+                                     c_int32, _P, POINTER(c_void_p)]),
+    "esr_bcg_graph_launch": (c_int, [_P, _P]),
+    "esr_bcg_graph_destroy": (c_int, [_P]),
     "esr_wait_selftest": (c_int, [c_int32, _P, _P]),
     "esr_gmres_workspace_bytes": (c_int64, [c_int64, c_int32]),
     "esr_gmres_init": (c_int, [POINTER(Sell), _P, c_double, c_double, _P, _P]),
@@ -135,7 +139,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 6
+ABI_VERSION = 7
 
 
 def library_path() -> Path:

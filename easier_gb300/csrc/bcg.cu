@@ -32,6 +32,8 @@
 // residual misses the tolerance continues from it: r = b - A x replaces the
 // recurrence residual and p keeps its direction (a residual replacement,
 // not a restart).
+#include <vector>
+
 #include "bcg_common.cuh"
 
 namespace {
@@ -435,7 +437,125 @@ int run_gnn_apply(const esr_batch *B, const void *r, void *z, void *ws, cudaStre
   return esr::gnn_layers(B, r, r, z, ws, s);
 }
 
+// ------------------------------------------------------------------------
+// The whole solve as ONE CUDA graph launch: [workspace memset, init] then a
+// device-side WHILE node whose body is [compaction + k iterations,
+// verification of the instances that converged in it, condition].  The
+// condition kernel keeps looping while instances run and stops after
+// max_bodies bodies whatever happens, so the graph always terminates.
+__global__ void bcg_graph_cond_kernel(cudaGraphConditionalHandle h, BcgHead *head, int max_bodies) {
+  const int bodies = head->bodies + 1;
+  head->bodies = bodies;
+  cudaGraphSetConditional(h, (head->active > 0 && bodies < max_bodies) ? 1u : 0u);
+}
+
+struct BcgGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+};
+
+template <class P>
+int build_graph(const esr_batch *B, const double *b64, const void *b, void *x, void *r, void *z, void *p, void *q,
+                double *x64, double *r64, double rtol, double atol, int32_t maxiter, int32_t k, void *ws,
+                BcgGraph *G) {
+  cudaError_t e = cudaStreamCreateWithFlags(&G->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaGraphCreate(&G->graph, 0);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create");
+  cudaStream_t s = G->capture;
+  // [memset, init]
+  e = cudaStreamBeginCaptureToGraph(s, G->graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/capture init");
+  int st = run_init<P>(B, b64, b, x, r, z, p, rtol, atol, maxiter, ws, s);
+  cudaGraph_t tmp = nullptr;
+  e = cudaStreamEndCapture(s, &tmp);
+  if (st) return st;
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/end init");
+  // the WHILE node after the init's last node
+  size_t nn = 0;
+  e = cudaGraphGetNodes(G->graph, nullptr, &nn);
+  if (e != cudaSuccess || nn == 0) return esr::cuda_check(e, "esr_bcg_graph_create/nodes");
+  std::vector<cudaGraphNode_t> nodes(nn), leaves;
+  e = cudaGraphGetNodes(G->graph, nodes.data(), &nn);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/nodes");
+  for (cudaGraphNode_t n : nodes) {
+    size_t nd = 0;
+    e = cudaGraphNodeGetDependentNodes(n, nullptr, nullptr, &nd);
+    if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/dependents");
+    if (nd == 0) leaves.push_back(n);
+  }
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, G->graph, 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/handle");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  e = cudaGraphAddNode(&cnode, G->graph, leaves.data(), nullptr, leaves.size(), &np);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/while node");
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  // the body
+  e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/capture body");
+  st = run_iterate<P>(B, x, r, z, p, q, k, ws, s);
+  if (!st) st = run_verify<P>(B, b64, x, x64, r64, r, z, p, ws, s);
+  const int max_bodies = (int)((maxiter + (int64_t)k) / k) * 2 + 16;  // replacements restart instances
+  if (!st) {
+    BcgLayout L = layout_of(ws, B->ninst, B->nchunks);
+    bcg_graph_cond_kernel<<<1, 1, 0, s>>>(h, L.head, max_bodies);
+  }
+  cudaGraph_t tmp2 = nullptr;
+  e = cudaStreamEndCapture(s, &tmp2);
+  if (st) return st;
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/end body");
+  e = cudaGraphInstantiate(&G->exec, G->graph, 0);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_create/instantiate");
+  return ESR_OK;
+}
+
+void destroy_graph(BcgGraph *G) {
+  if (!G) return;
+  if (G->exec) cudaGraphExecDestroy(G->exec);
+  if (G->graph) cudaGraphDestroy(G->graph);
+  if (G->capture) cudaStreamDestroy(G->capture);
+  delete G;
+}
+
 }  // namespace
+
+extern "C" int esr_bcg_graph_create(const esr_batch *B, const double *b64, const void *b, void *x, void *r, void *z,
+                                    void *p, void *q, double *x64, double *r64, double rtol, double atol,
+                                    int32_t maxiter, int32_t k, void *workspace, void **graph_out) {
+  int st = check_batch(B);
+  if (st) return st;
+  if (!b64 || !b || !x || !r || !z || !p || !q || !x64 || !r64 || !workspace || !graph_out)
+    return esr::fail(ESR_ERR_ARG, "null argument");
+  if (maxiter < 0 || maxiter > (1 << 26)) return esr::fail(ESR_ERR_ARG, "the one-launch graph needs a finite maxiter");
+  if (k < 1 || k > 1024) return esr::fail(ESR_ERR_ARG, "iterations per body must be in [1, 1024]");
+  BcgGraph *G = new BcgGraph();
+  st = B->df64 ? build_graph<PolDF>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G)
+               : build_graph<PolF64>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G);
+  if (st) {
+    destroy_graph(G);
+    return st;
+  }
+  *graph_out = G;
+  return ESR_OK;
+}
+
+extern "C" int esr_bcg_graph_launch(void *graph, void *stream) {
+  if (!graph) return esr::fail(ESR_ERR_ARG, "null graph");
+  cudaError_t e = cudaGraphLaunch(((BcgGraph *)graph)->exec, esr::as_stream(stream));
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_bcg_graph_launch");
+  return ESR_OK;
+}
+
+extern "C" int esr_bcg_graph_destroy(void *graph) {
+  destroy_graph((BcgGraph *)graph);
+  return ESR_OK;
+}
 
 extern "C" int esr_gnn_apply(const esr_batch *B, const void *r, void *z, void *workspace, void *stream) {
   int st = check_batch(B);

@@ -20,7 +20,8 @@ constexpr int kBSums = 3;       // partial arrays
 struct BcgHead {
   int32_t active;  // instances with done == 0
   int32_t acount;  // entries of the active chunk list
-  int32_t pad[62];
+  int32_t bodies;  // loop bodies run by the one-launch graph
+  int32_t pad[61];
 };
 
 struct BcgLayout {

@@ -204,6 +204,7 @@ class BatchedPCG:
         self.ws = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
         self.sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
         self._graphs = {}
+        self._one_graphs = {}
         self.kernel_launches = 0
         self.polls = 0
         self.tuning = None
@@ -241,6 +242,7 @@ class BatchedPCG:
                                _lib.ptr(self.inst_chunk0),
                                ctypes.pointer(self.gnn_desc) if self.gnn_desc is not None else None)
         self._graphs = {}
+        self._free_graphs()
 
     def bytes_per_row_iteration(self) -> float:
         """Algorithmic HBM bytes of one lockstep iteration per active packed
@@ -401,6 +403,39 @@ class BatchedPCG:
                     if bits & _lib.DEV_WAIT_TIMEOUT:
                         raise RuntimeError("a GNN tensor-core wait timed out on the device")
                 return rounds
+
+    # ------------------------------------------------- one-launch solve --
+    def solve_graph(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: int = 100000,
+                    k: Optional[int] = None) -> List[dict]:
+        """The whole solve as ONE CUDA graph launch (esr_bcg_graph_create):
+        init, then a device-side loop of k-iteration bodies with the FP64
+        verification, until no instance runs.  maxiter must be finite (it
+        also bounds the device loop).  The graph is built once per
+        (rtol, atol, maxiter, k) and work shape."""
+        k = int(k or self.graph_iters)
+        key = (float(rtol), float(atol or 0.0), int(maxiter), k, self.tiles_per_chunk, self.grid)
+        g = self._one_graphs.get(key)
+        if g is None:
+            h = ctypes.c_void_p()
+            _lib.call("esr_bcg_graph_create", ctypes.byref(self.desc), _lib.ptr(self.b64), _lib.ptr(self.b),
+                      _lib.ptr(self.x), _lib.ptr(self.r), _lib.ptr(self.z), _lib.ptr(self.p), _lib.ptr(self.q),
+                      _lib.ptr(self.x64), _lib.ptr(self.r64), float(rtol), float(atol) if atol else 0.0,
+                      int(maxiter), k, _lib.ptr(self.ws), ctypes.byref(h))
+            g = self._one_graphs[key] = h
+        _lib.call("esr_bcg_graph_launch", g, self._stream())
+        self.kernel_launches += 1
+        return [self._info(s) for s in self.instances()]
+
+    def _free_graphs(self):
+        for h in getattr(self, "_one_graphs", {}).values():
+            try:
+                _lib.call("esr_bcg_graph_destroy", h)
+            except Exception:  # interpreter shutdown
+                pass
+        self._one_graphs = {}
+
+    def __del__(self):
+        self._free_graphs()
 
     def solve(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: Optional[int] = None,
               max_rounds: int = 16) -> List[dict]:

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 6
+#define ESR_GB300_ABI_VERSION 7
 
 /* element types */
 enum {
@@ -590,6 +590,21 @@ int esr_bcg_iterate(const esr_batch *B, void *x, void *r, void *z, void *p,
 int esr_bcg_verify(const esr_batch *B, const double *b64, void *x, double *x64,
                    double *r64, void *r, void *z, void *p, void *workspace,
                    void *stream);
+
+/* The whole batched solve as ONE CUDA graph launch: workspace reset and
+ * esr_bcg_init, then a device-side WHILE node whose body is
+ * esr_bcg_iterate(k) + esr_bcg_verify and sets the loop condition on the
+ * device (instances still running).  maxiter must be finite: the loop also
+ * stops after 2*ceil(maxiter/k) + 16 bodies, so the graph always ends.
+ * Pointers and rtol/atol/maxiter are baked in at creation; launch with
+ * esr_bcg_graph_launch on any stream, free with esr_bcg_graph_destroy. */
+int esr_bcg_graph_create(const esr_batch *B, const double *b64, const void *b,
+                         void *x, void *r, void *z, void *p, void *q,
+                         double *x64, double *r64, double rtol, double atol,
+                         int32_t maxiter, int32_t k, void *workspace,
+                         void **graph_out);
+int esr_bcg_graph_launch(void *graph, void *stream);
+int esr_bcg_graph_destroy(void *graph);
 
 /* The GNN preconditioner alone: z = M(r) for every instance of a batch
  * with batch.gnn set (sigma = rms of each instance's r), zero on padding

@@ -84,3 +84,26 @@ def test_work_shapes_and_autotune_agree():
     eng.reset()
     res = eng.solve(rtol=1e-8)
     assert all(r["status"] == "converged" for r in res)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_one_graph_launch_solve_matches_polled_solve(precision):
+    """The whole batched solve as one CUDA graph launch (device-side loop)
+    gives the same iterations and solutions as the host-polled solve."""
+    insts = p1_instances(5, 8, 48, seed=21)
+    eng = BatchedPCG(insts, jacobi=True, precision=precision)
+    ref = eng.solve(rtol=1e-8, maxiter=5000)
+    x_ref = eng.solution().clone()
+    eng.reset()
+    res = eng.solve_graph(rtol=1e-8, maxiter=5000)
+    assert [r["iters"] for r in res] == [r["iters"] for r in ref]
+    assert all(r["status"] == "converged" for r in res)
+    assert torch.allclose(eng.solution(), x_ref, rtol=0, atol=0)
+    # replayed: same graph, same result
+    eng.reset()
+    res2 = eng.solve_graph(rtol=1e-8, maxiter=5000)
+    assert [r["iters"] for r in res2] == [r["iters"] for r in ref]
+    # a finite maxiter ends the device loop
+    eng.reset()
+    res3 = eng.solve_graph(rtol=1e-14, maxiter=7)
+    assert all(r["status"] == "maxiter" and r["iters"] == 7 for r in res3)
