@@ -376,6 +376,37 @@ def bench_poisson(args, world, rank, local):
         "gpu_launches": int(getattr(eng, "kernel_launches", 0) - launches0),
         "clocks": clk.summary(),
     }
+    # end to end through the public API: b from pinned host memory into the
+    # module's tensor, solve, x back to pinned host memory, every step
+    b_host = eqn.b.data.cpu().pin_memory()
+    x_host = torch.empty_like(b_host).pin_memory()
+    k_e2e = max(1, min(args.steps, 3))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        eqn.b.data.copy_(b_host, non_blocking=True)
+        eqn.x.data.zero_()
+        sol.solve(rtol=1e-8, precision=args.precision)
+        x_host.copy_(eqn.x.data, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+    nb = b_host.numel() * b_host.element_size()
+    line["e2e"] = {"value": world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+                   "path": "CG.solve on the compiled module, b in and x out through pinned host memory"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from easier_gb300 import mesh
+        from oracle import cg as ocg
+        s = mesh.p1_system(args.n)
+        bb = mesh.random_mode_rhs(args.n, 0)
+        k = 40
+        t0 = time.perf_counter()
+        ocg.cg(s.row, s.col, s.Ae, s.Av, bb, rtol=0.0, maxiter=k - 1, jacobi=True)
+        per_it = (time.perf_counter() - t0) / k
+        line["cpu_baseline"] = {"value": 1.0 / (per_it * (nit + 1)), "unit": "solves/s",
+                                "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": f"{k} oracle Jacobi-PCG iterations on the {args.n}x{args.n} P1 system "
+                                          f"({per_it * 1e3:.1f} ms each), scaled to the {nit:.0f} iterations of a "
+                                          f"solve"}
     return line
 
 

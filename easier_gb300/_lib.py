@@ -77,7 +77,8 @@ class BcgInst(Structure):
                 ("sigma", c_double), ("rr_mark", c_double), ("rz_jac", c_double), ("theta", c_double),
                 ("iters", c_int32), ("done", c_int32), ("verified", c_int32), ("restarts", c_int32),
                 ("maxiter", c_int32), ("mode", c_int32), ("refresh", c_int32), ("fallbacks", c_int32),
-                ("nrows", c_int32), ("gnn_iters", c_int32), ("clips", c_int32), ("clips_mark", c_int32)]
+                ("nrows", c_int32), ("gnn_iters", c_int32), ("clips", c_int32), ("clips_mark", c_int32),
+                ("alpha_df", ctypes.c_float * 2), ("beta_df", ctypes.c_float * 2)]
 
 
 _P = c_void_p
@@ -139,7 +140,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 7
+ABI_VERSION = 8
 
 
 def library_path() -> Path:

@@ -90,7 +90,7 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     rz.add(ri, zi);
     rr.add(ri, ri);
   }
-  const double v[3] = {bb, rz.value(), rr.value()};
+  const double v[3] = {bsum<kBThreads>(DotAccD{bb}), bsum<kBThreads>(rz), bsum<kBThreads>(rr)};
   double tot[3];
   if (tile_finish<3>(a, inst, v, L, tot) && threadIdx.x == 0) {
     esr_bcg_inst &s = L.inst[inst];
@@ -100,7 +100,9 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     s.tol = tol;
     s.rz = tot[1];
     s.rr = tot[2];
-    s.pq = s.alpha = s.beta = 0.0;
+    s.pq = 0.0;
+    set_alpha(s, 0.0);
+    set_beta(s, 0.0);
     s.true_rr = -1.0;
     s.iters = 0;
     s.verified = 0;
@@ -143,7 +145,7 @@ bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
       q[i] = qi;
       pq.add(pi, qi);
     }
-    const double v[1] = {pq.value()};
+    const double v[1] = {bsum<kBThreads>(pq)};
     double tot[1];
     if (chunk_finish<1>(a, c, inst, v, L, tot) && threadIdx.x == 0) {
       esr_bcg_inst &s = L.inst[inst];
@@ -152,7 +154,7 @@ bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
         s.done = 3;  // breakdown
         retire(L);
       } else {
-        s.alpha = s.rz / tot[0];
+        set_alpha(s, s.rz / tot[0]);
       }
     }
   }
@@ -170,9 +172,8 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
     const int c = L.alist[w];
     const int inst = a.chunk_inst[c];
     if (L.inst[inst].done) continue;
-    const double ad = L.inst[inst].alpha;
     const bool gnn = L.inst[inst].mode == kModeGnn;  // z comes from the GNN layers
-    const V av = P::of(ad), nav = P::of(-ad);
+    const V av = P::alpha(L.inst[inst]), nav = P::neg(av);
     typename P::Acc rr, rz;
     const int t1 = a.chunk_tile0[c + 1];
 #pragma unroll 2
@@ -186,7 +187,7 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
       rr.add(ri, ri);
       rz.add(ri, zi);
     }
-    const double v[2] = {rr.value(), rz.value()};
+    const double v[2] = {bsum<kBThreads>(rr), bsum<kBThreads>(rz)};
     double tot[2];
     if (chunk_finish<2>(a, c, inst, v, L, tot) && threadIdx.x == 0) {
       esr_bcg_inst &s = L.inst[inst];
@@ -216,14 +217,14 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
             s.refresh = 1;
             s.fallbacks += 1;
             s.gnn_iters = s.iters;
-            s.beta = 0.0;
+            set_beta(s, 0.0);
             s.rz = tot[1];
           } else {
             s.rr_mark = tot[0];
           }
         }
       } else {
-        s.beta = tot[1] / s.rz;
+        set_beta(s, tot[1] / s.rz);
         s.rz = tot[1];
       }
     }
@@ -242,11 +243,15 @@ bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, const typename 
     const int c = L.alist[w];
     const int inst = a.chunk_inst[c];
     if (L.inst[inst].done) continue;
-    const V beta = P::of(L.inst[inst].beta);
+    const V beta = P::beta(L.inst[inst]);
     const bool refresh = L.inst[inst].refresh != 0;
     const double theta = L.inst[inst].theta;
     const bool blend = L.inst[inst].mode == kModeGnn && theta != 1.0;
-    const V th = P::of(theta), omth = P::of(1.0 - theta);
+    V th = P::zero(), omth = P::zero();
+    if (blend) {
+      th = P::of(theta);
+      omth = P::of(1.0 - theta);
+    }
     const int t1 = a.chunk_tile0[c + 1];
 #pragma unroll 2
     for (int t = a.chunk_tile0[c]; t < t1; ++t) {
@@ -290,7 +295,7 @@ bcg_residual_kernel(BArgs a, const double *__restrict__ val64, const double *__r
     r64[i] = ri;
     rr = ri * ri;
   }
-  const double v[1] = {rr};
+  const double v[1] = {bsum<kBThreads>(DotAccD{rr})};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
     st.true_rr = tot[0];
@@ -318,11 +323,11 @@ bcg_replace_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const dou
     z[i] = zi;
     rz.add(ri, zi);
   }
-  const double v[1] = {rz.value()};
+  const double v[1] = {bsum<kBThreads>(rz)};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
     // GNN mode: p restarts from the Jacobi direction (beta = 0)
-    st.beta = (st.mode != kModeGnn && st.rz != 0.0) ? tot[0] / st.rz : 0.0;
+    set_beta(st, (st.mode != kModeGnn && st.rz != 0.0) ? tot[0] / st.rz : 0.0);
     st.rz = tot[0];
     st.rz_jac = tot[0];
     st.rr = st.true_rr;
@@ -337,7 +342,7 @@ bcg_replace_p_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V
   esr_bcg_inst &st = L.inst[inst];
   if (st.verified != -2) return;
   const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
-  if (i < a.n) p[i] = P::fma(P::of(st.beta), p[i], z[i]);
+  if (i < a.n) p[i] = P::fma(P::beta(st), p[i], z[i]);
   // the instance's tiles all pass the test above before any of them
   // re-arms it: the ticket counter orders them
   const double v[1] = {0.0};
@@ -359,7 +364,7 @@ gnn_prep_kernel(BArgs a, const typename P::V *__restrict__ r, BcgLayout L) {
   const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
   typename P::Acc rr;
   if (i < a.n) rr.add(r[i], r[i]);
-  const double v[1] = {rr.value()};
+  const double v[1] = {bsum<kBThreads>(rr)};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
     esr_bcg_inst &s = L.inst[inst];
@@ -367,7 +372,7 @@ gnn_prep_kernel(BArgs a, const typename P::V *__restrict__ r, BcgLayout L) {
     s.sigma = s.nrows > 0 ? sqrt(tot[0] / s.nrows) : 0.0;
     s.rr = tot[0];
     s.rz = 1.0;
-    s.alpha = 0.0;
+    set_alpha(s, 0.0);
     s.mode = kModeGnn;
     s.done = 0;
   }

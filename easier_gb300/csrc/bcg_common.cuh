@@ -73,9 +73,67 @@ struct DotAccDF {  // hi*hi products exactly (two-prod + two-sum), cross terms i
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// alpha and beta of an instance, kept in both forms (set once per
+// iteration by the finishing thread; the df64 kernels read the float pair)
+__device__ __forceinline__ void split_df(double v, float (&out)[2]) {
+  const float hi = __double2float_rn(v);
+  out[0] = hi;
+  out[1] = __double2float_rn(v - (double)hi);
+}
+__device__ __forceinline__ void set_alpha(esr_bcg_inst &s, double a) {
+  s.alpha = a;
+  split_df(a, s.alpha_df);
+}
+__device__ __forceinline__ void set_beta(esr_bcg_inst &s, double b) {
+  s.beta = b;
+  split_df(b, s.beta_df);
+}
+
+// Block sum of a per-thread dot accumulator (identical result in every
+// thread, fixed order).  FP64: shuffles of doubles.  df64: the (hi, lo)
+// pairs are added with the double-float add on the FP32 pipes and only the
+// block total is widened to double, so the df64 kernels issue no FP64
+// arithmetic per chunk.
+template <int THREADS>
+__device__ __forceinline__ double bsum(const DotAccD &a) {
+  __shared__ double s_red[THREADS / 32];
+  return esr::block_sum_fixed<THREADS>(a.v, s_red);
+}
+
+__device__ __forceinline__ df64::df warp_sum_df(df64::df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const df64::df w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    v = df64::add(v, w);
+  }
+  return v;
+}
+
+template <int THREADS>
+__device__ __forceinline__ double bsum(const DotAccDF &a) {
+  __shared__ float2 s_red[THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  df64::df v = df64::quick_two_sum(a.hi, a.lo);
+  v = warp_sum_df(v);
+  if (lane == 0) s_red[warp] = make_float2(v.hi, v.lo);
+  __syncthreads();
+  if (warp == 0) {
+    const float2 t = lane < THREADS / 32 ? s_red[lane] : make_float2(0.f, 0.f);
+    v = warp_sum_df(df64::df{t.x, t.y});
+    if (lane == 0) s_red[0] = make_float2(v.hi, v.lo);
+  }
+  __syncthreads();
+  const float2 t = s_red[0];
+  __syncthreads();
+  return (double)t.x + (double)t.y;
+}
+
 struct PolF64 {
   using V = double;
   using Acc = DotAccD;
+  static __device__ __forceinline__ V alpha(const esr_bcg_inst &s) { return s.alpha; }
+  static __device__ __forceinline__ V beta(const esr_bcg_inst &s) { return s.beta; }
+  static __device__ __forceinline__ V neg(V a) { return -a; }
   static __device__ __forceinline__ V fma(V a, V b, V c) { return ::fma(a, b, c); }
   static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
   static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
@@ -89,6 +147,9 @@ struct PolF64 {
 struct PolDF {
   using V = df64::df;
   using Acc = DotAccDF;
+  static __device__ __forceinline__ V alpha(const esr_bcg_inst &s) { return V{s.alpha_df[0], s.alpha_df[1]}; }
+  static __device__ __forceinline__ V beta(const esr_bcg_inst &s) { return V{s.beta_df[0], s.beta_df[1]}; }
+  static __device__ __forceinline__ V neg(V a) { return df64::neg(a); }
   static __device__ __forceinline__ V fma(V a, V b, V c) { return df64::fma(a, b, c); }
   static __device__ __forceinline__ V mul(V a, V b) { return df64::mul(a, b); }
   static __device__ __forceinline__ V sub(V a, V b) { return df64::add(a, df64::neg(b)); }
@@ -162,14 +223,12 @@ __device__ __forceinline__ double bsell_row64(int64_t i, int64_t n, const int64_
 // counter; the CTA holding the last of `expected` tickets (returns true in
 // all its threads) adds partial[k][p0..p1) in order into tot and resets the
 // counter.  Never waits on another CTA.
+// `bs` are the block's sums (bsum above, the same in every thread).
 template <int K, int THREADS = kBThreads>
-__device__ __forceinline__ bool inst_finish(const double (&v)[K], int slot, int p0, int p1, int expected,
+__device__ __forceinline__ bool inst_finish(const double (&bs)[K], int slot, int p0, int p1, int expected,
                                             int nblocks, double *partial, unsigned int *counter, double (&tot)[K]) {
   __shared__ double s_red[THREADS / 32];
   __shared__ bool s_last;
-  double bs[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) bs[k] = esr::block_sum_fixed<THREADS>(v[k], s_red);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) partial[k * (int64_t)nblocks + slot] = bs[k];

@@ -335,7 +335,7 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
     }
     if (stop) break;
     if (LAYER == 4) {
-      const double v[3] = {nr.value(), nq.value(), jq.value()};
+      const double v[3] = {bsum<kGThreads>(nr), bsum<kGThreads>(nq), bsum<kGThreads>(jq)};
       double tot[3];
       if (chunk_finish<3, kGThreads>(a, c, inst, v, L, tot) && tid == 0) {
         esr_bcg_inst &s = L.inst[inst];
@@ -354,10 +354,10 @@ gnn_layer_kernel(BArgs a, GArgs g, const typename P::V *__restrict__ r, const ty
           s.refresh = 1;
           s.fallbacks += 1;
           s.gnn_iters = s.iters;
-          s.beta = 0.0;
+          set_beta(s, 0.0);
           s.rz = s.rz_jac;
         } else {
-          s.beta = -s.alpha * zq / s.rz;
+          set_beta(s, -s.alpha * zq / s.rz);
           s.rz = zr;
         }
       }

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 7
+#define ESR_GB300_ABI_VERSION 8
 
 /* element types */
 enum {
@@ -564,6 +564,8 @@ typedef struct {
   int32_t gnn_iters; /* iteration of the last GNN -> Jacobi switch (0 none) */
   int32_t clips;     /* iterations with theta < 1                           */
   int32_t clips_mark;/* clips at the last stall check                       */
+  float alpha_df[2]; /* alpha and beta as double-float pairs (hi, lo), set   */
+  float beta_df[2];  /* with alpha/beta so the df64 kernels need no FP64 op */
 } esr_bcg_inst;
 
 int64_t esr_bcg_workspace_bytes(int32_t ninst, int32_t nblocks,
