@@ -9,18 +9,20 @@ import torch
 from .sparse import linsys_apply
 
 
-def cg(row, col, Ae, Av, b, x0=None, rtol=1e-5, atol=None, maxiter=None, jacobi=False):
-    Ae, Av, b = (torch.as_tensor(a, dtype=torch.float64) for a in (Ae, Av, b))
+def cg(row, col, Ae, Av, b, x0=None, rtol=1e-5, atol=None, maxiter=None, jacobi=False, dtype=torch.float64):
+    """``dtype`` = the system's dtype (the reference computes in the module's
+    dtype: FP64 by default, FP32 after ``Module.to(torch.float32)``)."""
+    Ae, Av, b = (torch.as_tensor(a).to(dtype) for a in (Ae, Av, b))
     A = lambda v: linsys_apply(v, row, col, Ae, Av)  # noqa: E731
     M = (lambda r: r / Av) if jacobi else (lambda r: r)  # noqa: E731
-    x = torch.zeros_like(b) if x0 is None else torch.as_tensor(x0, dtype=torch.float64).clone()
+    x = torch.zeros_like(b) if x0 is None else torch.as_tensor(x0).to(dtype).clone()
     r = b - A(x)
     z = M(r)
     p = z.clone()
     bnorm = torch.linalg.vector_norm(b)
     tol = rtol * bnorm
     if atol:
-        tol = max(tol, torch.tensor(atol, dtype=torch.float64))
+        tol = max(tol, torch.tensor(atol, dtype=dtype))
     iters = 0
     while True:
         Ap = A(p)

@@ -167,3 +167,28 @@ def test_fused_gmres_maxiter():
     [eqn, sol] = esr.compile([eqn, sol], "cuda")
     info = sol.solve(rtol=1e-12, maxiter=3)
     assert info["iters"] == 3 and info["residual"] > 0
+
+
+def test_fp32_system_uses_single_system_kernels():
+    """An FP32 Linsys solves on the single-system PCG kernels (float
+    vectors, (hi, lo) float-pair dot accumulation) and reaches the FP32
+    tolerance against the FP64 oracle."""
+    from easier_gb300.numeric.sparse import FusedPCG
+    eqn = workloads.P1Poisson(48, rhs_seed=7)
+    eqn.to(torch.float32)
+    sol = CG(eqn.A, eqn.b, eqn.x, M=Jacobi(eqn.A))
+    [eqn, sol] = esr.compile([eqn, sol], "cuda")
+    assert eqn.x.dtype == torch.float32 and sol.r.dtype == torch.float32
+    info = sol.solve(rtol=1e-5, maxiter=5000)
+    assert isinstance(sol._fused, FusedPCG) and info["status"] == "converged"
+    s = mesh.p1_system(48)
+    b = mesh.random_mode_rhs(48, 7)
+    x_ref, it_ref, _ = ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-5, maxiter=5000, jacobi=True)
+    _, it32, _ = ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-5, maxiter=5000, jacobi=True, dtype=torch.float32)
+    # the FP32 recurrence (reference order, FP32 tensors) takes more
+    # iterations than FP64 on this few-mode right hand side
+    assert abs(info["iters"] - it32) <= max(3, it32 // 10), (info["iters"], it32, it_ref)
+    x = eqn.x.collect().double().cpu().numpy()
+    assert np.linalg.norm(x - x_ref.numpy()) <= 1e-3 * np.linalg.norm(x_ref.numpy())
+    tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, b, x)
+    assert tr <= 2e-5 * np.linalg.norm(b)
