@@ -209,6 +209,9 @@ def bench_swe(args, world, rank, local):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     eqn = workloads.make_swe(args.n, dt=args.dt, dtype=dtype)
+    if args.tile_cells:
+        from easier_gb300 import swe
+        swe.DEFAULT_TILE_CELLS = args.tile_cells
     [eqn] = esr.compile([eqn], "cuda", precision=args.precision)
     eng = eqn.easier_fused_engine
     if eng is None:
@@ -701,6 +704,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--tile-cells", type=int, default=None, help="swe: target cells per tile (FP32 tiled step)")
     args = ap.parse_args()
     if args.n is None:
         args.n = 2000 if args.workload == "swe" else 1000

@@ -106,6 +106,7 @@ _SIGS = {
     "esr_swe_step": (c_int, [POINTER(SweMesh), c_double, _P, c_int64, _P, _P]),
     "esr_swe_delta": (c_int, [POINTER(SweMesh), _P, _P, _P]),
     "esr_swe_tile_smem_bytes": (c_int64, [POINTER(SweTiles)]),
+    "esr_swe_tile_threads": (c_int, [POINTER(SweTiles)]),
     "esr_swe_tile_step": (c_int, [POINTER(SweTiles), c_double, _P, _P, c_int64, _P]),
     "esr_bisect_partition": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P]),
     "esr_swe_tile_layout": (c_int, [c_int64, _P, _P, c_int64, _P, POINTER(c_int64), POINTER(c_int64), _P, _P, _P,

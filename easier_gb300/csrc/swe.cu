@@ -299,10 +299,14 @@ int dispatch_delta(const esr_swe_mesh *m, const void *state, void *delta, cudaSt
 // the result is bitwise the same for the same EXACT setting.  HBM traffic
 // per step is the tile's geometry (plus the halo's), s0 of tile + halo, and
 // the new state; the stage states never leave the SM.
-constexpr int kTileThreads = 1024;
-constexpr int kTileIters = 6;     // cells of level <= 3 per thread: <= 6 * 1024
-constexpr int kTileOwnIters = 4;  // tile cells per thread: <= 4 * 1024
+// The CTA size TT is 1024, 512 or 256 threads with 1024 / TT CTAs per SM
+// (64 registers a thread either way): the largest tiles use one CTA per SM,
+// tiles of half or a quarter the size run two or four CTAs per SM, so one
+// CTA's state loads and barriers overlap another's compute.
+constexpr int kTileIters = 6;     // cells of level <= 3 per thread: <= 6 * TT
+constexpr int kTileOwnIters = 4;  // tile cells per thread: <= 4 * TT
 constexpr int kTileGroup = 2;     // cells whose geometry loads are issued together
+constexpr int kTileMaxThreads = 1024;
 
 struct SlotsT {  // one tile's face slots, [3][n3] records {sx, sy, alpha, lnbr}
   const float4 *slot;
@@ -387,11 +391,11 @@ __device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &
   }
 }
 
-// Cells j = tid + r * kTileThreads in groups of kTileGroup consecutive r:
+// Cells j = tid + r * TT in groups of kTileGroup consecutive r:
 // the geometry of the whole group is requested before any of its cells is
 // computed, so the group's loads are in flight together (the kernel is
 // latency-bound on these L1/L2 loads otherwise).
-template <int STAGE, bool EXACT>
+template <int TT, int STAGE, bool EXACT>
 __device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, const float *hs, const float *us,
                                            const float *vs, const float *h0, const float *u0, const float *v0,
                                            float *ho, float *uo, float *vo, float (&acc)[kTileOwnIters][3],
@@ -402,12 +406,12 @@ __device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, c
     CellGeom cg[kTileGroup];
 #pragma unroll
     for (int u = 0; u < kTileGroup; ++u) {
-      const int j = threadIdx.x + (r0 + u) * kTileThreads;
+      const int j = threadIdx.x + (r0 + u) * TT;
       if (r0 + u < kIters && j < count) load_geom<EXACT>(j, g, cg[u]);
     }
 #pragma unroll
     for (int u = 0; u < kTileGroup; ++u) {
-      const int j = threadIdx.x + (r0 + u) * kTileThreads;
+      const int j = threadIdx.x + (r0 + u) * TT;
       if (r0 + u < kIters && j < count)
         tile_cell<STAGE, EXACT>(r0 + u, j, n0, cg[u], g.nL, hs, us, vs, h0, u0, v0, ho, uo, vo, acc, c, sout,
                                 cell_off);
@@ -415,8 +419,8 @@ __device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, c
   }
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(kTileThreads, 1)
+template <bool EXACT, int TT>
+__global__ void __launch_bounds__(TT, kTileMaxThreads / TT)
 swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
                      const float4 *__restrict__ gslot, const float *__restrict__ garea,
@@ -431,7 +435,7 @@ swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   float *hA = v0 + max_local, *uA = hA + max_l3, *vA = uA + max_l3;
   float *hB = vA + max_l3, *uB = hB + max_l3, *vB = uB + max_l3;
   const int64_t hb = offh[t];
-  for (int j = threadIdx.x; j < nL; j += kTileThreads) {
+  for (int j = threadIdx.x; j < nL; j += TT) {
     const int64_t gcell = j < n0 ? (int64_t)cell_off + j : (int64_t)__ldg(halo + hb + (j - n0));
     if (gcell < 0 || gcell >= nc) {  // corrupt layout: flag, never read out of bounds
       esr::raise_status(ESR_DEV_IDX_RANGE);
@@ -451,13 +455,13 @@ swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   float acc[kTileOwnIters][3];
 #pragma unroll
   for (int r = 0; r < kTileOwnIters; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.f;
-  tile_stage<1, EXACT>(n3, n0, g, h0, u0, v0, h0, u0, v0, hA, uA, vA, acc, c1, sout, cell_off);
+  tile_stage<TT, 1, EXACT>(n3, n0, g, h0, u0, v0, h0, u0, v0, hA, uA, vA, acc, c1, sout, cell_off);
   __syncthreads();
-  tile_stage<2, EXACT>(n2, n0, g, hA, uA, vA, h0, u0, v0, hB, uB, vB, acc, c1, sout, cell_off);
+  tile_stage<TT, 2, EXACT>(n2, n0, g, hA, uA, vA, h0, u0, v0, hB, uB, vB, acc, c1, sout, cell_off);
   __syncthreads();
-  tile_stage<3, EXACT>(n1, n0, g, hB, uB, vB, h0, u0, v0, hA, uA, vA, acc, c3, sout, cell_off);
+  tile_stage<TT, 3, EXACT>(n1, n0, g, hB, uB, vB, h0, u0, v0, hA, uA, vA, acc, c3, sout, cell_off);
   __syncthreads();
-  tile_stage<4, EXACT>(n0, n0, g, hA, uA, vA, h0, u0, v0, nullptr, nullptr, nullptr, acc, c4, sout, cell_off);
+  tile_stage<TT, 4, EXACT>(n0, n0, g, hA, uA, vA, h0, u0, v0, nullptr, nullptr, nullptr, acc, c4, sout, cell_off);
 }
 
 int64_t tile_smem_bytes(const esr_swe_tiles *T) {
@@ -468,9 +472,9 @@ int check_tiles(const esr_swe_tiles *T) {
   if (!T) return esr::fail(ESR_ERR_ARG, "null tile layout");
   if (T->dtype != ESR_F32) return esr::fail(ESR_ERR_UNSUPPORTED, "tiled step is FP32 only");
   if (T->nc <= 0 || T->ntiles <= 0) return esr::fail(ESR_ERR_ARG, "empty tile layout");
-  if (T->max_own > kTileOwnIters * kTileThreads)
+  if (T->max_own > kTileOwnIters * kTileMaxThreads)
     return esr::fail(ESR_ERR_UNSUPPORTED, "a tile has more than 4096 cells");
-  if (T->max_l3 > kTileIters * kTileThreads)
+  if (T->max_l3 > kTileIters * kTileMaxThreads)
     return esr::fail(ESR_ERR_UNSUPPORTED, "a tile plus 3 halo rings has more than 6144 cells");
   if (T->max_local < T->max_l3 || T->max_l3 < T->max_own) return esr::fail(ESR_ERR_ARG, "inconsistent tile maxima");
   if (tile_smem_bytes(T) > 227 * 1024) return esr::fail(ESR_ERR_UNSUPPORTED, "tile needs more than 227 KB shared memory");
@@ -480,22 +484,45 @@ int check_tiles(const esr_swe_tiles *T) {
   return ESR_OK;
 }
 
-template <bool EXACT>
-int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps, cudaStream_t s) {
+// CTA size for a tile layout: the smallest that holds the largest tile
+// (4 own cells and 6 level-<=3 cells a thread) and whose 1024 / TT CTAs fit
+// one SM's shared memory together (228 KB, 1 KB of it reserved per CTA).
+int tile_threads(const esr_swe_tiles *T) {
+  const int64_t smem = tile_smem_bytes(T);
+  for (int tt = 256; tt < kTileMaxThreads; tt *= 2) {
+    const int64_t ctas = kTileMaxThreads / tt;
+    if (T->max_own <= kTileOwnIters * tt && T->max_l3 <= kTileIters * tt && ctas * (smem + 1024) <= 228 * 1024)
+      return tt;
+  }
+  return kTileMaxThreads;
+}
+
+template <bool EXACT, int TT>
+int run_tiles_tt(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
+                 cudaStream_t s) {
   const int64_t smem = tile_smem_bytes(tiles);
-  cudaError_t e = cudaFuncSetAttribute(swe_tile_step_kernel<EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(swe_tile_step_kernel<EXACT, TT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/smem attribute");
   const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
   float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
   for (int64_t k = 0; k < steps; ++k) {
-    swe_tile_step_kernel<EXACT><<<tiles->ntiles, kTileThreads, smem, s>>>(
+    swe_tile_step_kernel<EXACT, TT><<<tiles->ntiles, TT, smem, s>>>(
         tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots,
         (const float *)tiles->area, (const float *)tiles->inv_area, buf[k & 1], buf[(k + 1) & 1], tiles->nc,
         tiles->max_local, tiles->max_l3, c1, c3, c4);
   }
   ESR_LAUNCH_CHECK("esr_swe_tile_step");
   return ESR_OK;
+}
+
+template <bool EXACT>
+int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps, cudaStream_t s) {
+  switch (tile_threads(tiles)) {
+    case 256: return run_tiles_tt<EXACT, 256>(tiles, dt, state_a, state_b, steps, s);
+    case 512: return run_tiles_tt<EXACT, 512>(tiles, dt, state_a, state_b, steps, s);
+    default: return run_tiles_tt<EXACT, 1024>(tiles, dt, state_a, state_b, steps, s);
+  }
 }
 
 }  // namespace
@@ -540,6 +567,11 @@ extern "C" int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *
 extern "C" int64_t esr_swe_tile_smem_bytes(const esr_swe_tiles *tiles) {
   if (check_tiles(tiles)) return -1;
   return tile_smem_bytes(tiles);
+}
+
+extern "C" int esr_swe_tile_threads(const esr_swe_tiles *tiles) {
+  if (check_tiles(tiles)) return -1;
+  return tile_threads(tiles);
 }
 
 extern "C" int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,

@@ -51,6 +51,11 @@ REDUCERS = ("scatter", "scatter_b")
 STATE = ("h", "uh", "vh")
 
 TILE_CELLS = 4096       # tile size cap (kernel limit: 4096 own cells)
+TILE_MIN_CELLS = 256
+# Target tile size; None = auto: one tile per SM while the mesh is small,
+# TILE_CELLS on large meshes.  Tiles of <= 1024 / 2048 own cells run 4 / 2
+# CTAs per SM.
+DEFAULT_TILE_CELLS: Optional[int] = None
 TILE_MAX_L3 = 6144      # kernel limit on tile + 3 halo rings
 TILE_SMEM = 227 * 1024  # shared memory per CTA
 DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
@@ -111,9 +116,15 @@ class SweEngine:
         self.dtype = binding["dtype"]
         self.device = binding["tensors"]["h"].device
         self.nc = binding["nc"]
-        self.tile_cells = tile_cells or TILE_CELLS
+        self.tile_cells = min(tile_cells or DEFAULT_TILE_CELLS or self._auto_tile_cells(), TILE_CELLS)
         self.mode = mode
         self._build_layout()
+
+    def _auto_tile_cells(self) -> int:
+        """Largest tiles (least halo work) while there are enough of them to
+        give every SM one."""
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count if self.device.type == "cuda" else 1
+        return max(TILE_MIN_CELLS, min(TILE_CELLS, -(-self.nc // sms)))
 
     # ----------------------------------------------------------- layout --
     def _build_layout(self) -> None:
@@ -286,13 +297,18 @@ class SweEngine:
     def launches_per_step(self) -> int:
         return 1 if self.tiled else 4
 
+    def tile_threads(self) -> int:
+        """Threads per CTA of the tiled step (1024 / that many CTAs per SM)."""
+        return int(_lib.lib().esr_swe_tile_threads(ctypes.byref(self._tiles))) if self.tiled else 0
+
     def describe(self) -> str:
         s = (f"nc={self.nc} width={self.width} dtype={str(self.dtype).replace('torch.', '')} "
              f"kernel={'tiled' if self.tiled else 'staged'} precision={self.precision} reorder={self.reorder}")
         if self.tiled:
             st = self.tile_stats
             s += (f" tiles={st['ntiles']} own<={st['max_own']} L3/own={st['l3_over_own']:.3f}"
-                  f" local/own={st['local_over_own']:.3f} smem={st['smem']}")
+                  f" local/own={st['local_over_own']:.3f} smem={st['smem']}"
+                  f" cta={self.tile_threads()}")
         return s
 
     def touched_bytes_per_step(self) -> int:

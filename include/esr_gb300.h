@@ -290,6 +290,11 @@ typedef struct {
  * outside the limits. */
 int64_t esr_swe_tile_smem_bytes(const esr_swe_tiles *tiles);
 
+/* Threads per CTA esr_swe_tile_step launches for this layout (1024, 512 or
+ * 256, with 1024 / threads CTAs resident per SM), or -1 if the layout is
+ * outside the limits. */
+int esr_swe_tile_threads(const esr_swe_tiles *tiles);
+
 /* `steps` steps of swe_main.py:121-141, one launch per step, bitwise equal
  * to esr_swe_step with the same `exact` setting.  Step k reads buffer k%2 and writes the other
  * ([nc][4] FP32 each, tile-major numbering): the result is in state_a when

@@ -133,9 +133,12 @@ def test_delta_matches_oracle():
         assert torch.equal(got, ref[j])
 
 
-@pytest.mark.parametrize("n", [37, 150])
-def test_tiled_equals_staged_fp32(n, monkeypatch):
+@pytest.mark.parametrize("n,tile,cta", [(37, 4096, 1024), (150, 4096, 1024), (150, 2048, 512), (150, 1024, 256)])
+def test_tiled_equals_staged_fp32(n, tile, cta, monkeypatch):
+    """The tiled step (each CTA size: 1, 2 or 4 CTAs per SM) is bitwise the
+    staged step."""
     from easier_gb300 import swe
+    monkeypatch.setattr(swe, "DEFAULT_TILE_CELLS", tile)
     outs = []
     for mode in ("tiled", "staged"):
         monkeypatch.setattr(swe, "DEFAULT_MODE", mode)
@@ -143,6 +146,8 @@ def test_tiled_equals_staged_fp32(n, monkeypatch):
         [eqn] = esr.compile([eqn], "cuda")
         eng = eqn.easier_fused_engine
         assert eng.tiled == (mode == "tiled")
+        if eng.tiled:
+            assert eng.tile_threads() == cta
         eng.step(7)
         eqn()
         outs.append([getattr(eqn, k).collect().cpu() for k in ("h", "uh", "vh")])
