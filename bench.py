@@ -180,6 +180,25 @@ def swe_secondary(args, eng32, dev, stream):
                               "bound": "fp64 pipe (GB300 FP64 rate is 1/59 of FP32)"}
     del eqn, eng
     torch.cuda.empty_cache()
+    # the module's own forward on the per-op path (compile(fuse=False)): the
+    # reference's op sequence with its Selector/Reducer calls on the gather /
+    # segmented-reduce kernels and the elementwise glue in torch
+    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=torch.float64)
+    [eqn] = esr.compile([eqn], "cuda", fuse=False)
+    steps = 3
+    eqn()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        eqn()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    out["f64_per_op"] = {"value": eqn.nc * steps / (ms / 1e3), "unit": "cell-steps/s", "steps": steps,
+                         "ms_per_step": ms / steps, "path": "module forward, one kernel per op"}
+    del eqn
+    torch.cuda.empty_cache()
     return out
 
 
@@ -490,7 +509,8 @@ def bench_batched(args, world, rank, local):
     else:  # kernels the device-side loop ran: init, then per body compaction, k iterations, verification
         kk = eng.graph_iters
         bodies = -(-(max(r["iters"] for r in res) + 1) // kk)
-        launches = args.steps * (1 + bodies * (1 + 3 * kk + 4 + 1))
+        per_it = 2 if eng.precision == "df64" else 3
+        launches = args.steps * (1 + bodies * (1 + per_it * kk + 4 + 1))
     bad = [i for i, r in enumerate(res) if r["status"] != "converged" or not r["true_residual"] <= 1e-8 * r["bnorm"]
            * 1.0001]
     if bad:

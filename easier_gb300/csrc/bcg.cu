@@ -12,8 +12,12 @@
 // Work decomposition.  Every instance is padded to whole 256-row tiles
 // (identity rows), so no tile spans two instances.  Consecutive tiles of an
 // instance form chunks of up to `tiles_per_chunk` tiles: the unit of work
-// of one CTA iteration in the three per-iteration kernels, which are
-// persistent (a fixed grid loops over the chunk list).  A one-CTA compaction
+// of one CTA iteration in the per-iteration kernels, which are persistent
+// (a fixed grid loops over the chunk list): the direction sweep (p, q = A p,
+// p.q) and the update sweep (x, r, z, r.r, r.z), plus the GNN layers and a
+// z fix-up in GNN batches.  The double-float policy forms the direction in
+// one sweep (q = A z + beta q); the FP64 policy, bound by the FP64 pipe,
+// keeps q = A p and a separate p-update sweep at the end of the iteration.  A one-CTA compaction
 // kernel at the start of every esr_bcg_iterate call lists the chunks of the
 // instances still running, so finished instances cost nothing afterwards.
 // Each dot product is finished per instance by the instance's last chunk to
@@ -109,7 +113,7 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
     s.restarts = 0;
     s.maxiter = maxiter;
     s.mode = a.use_gnn ? kModeGnn : kModeJacobi;
-    s.refresh = 0;
+    s.refresh = 2;  // the first direction: p = z, q = A z
     s.fallbacks = 0;
     s.gnn_iters = 0;
     s.clips = 0;
@@ -124,7 +128,56 @@ bcg_init_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
   }
 }
 
-// ---- step part 1: q = A p; p.q; alpha
+// ---- step part 1: the direction and its product with A.
+// p = z + beta p and q = A p, formed as q = A z + beta q (A p_new =
+// A z + beta A p_old): the SpMV reads z, which the previous sweep finished,
+// so the p-update needs no sweep of its own; then p.q -> alpha.  Each row
+// reads other rows' z (never written here) and writes only its own p and q.
+// A first direction (refresh != 0: after init or a residual replacement,
+// and the GNN's fallback to Jacobi) is p = z, q = A z.  The GNN's clipped
+// correction is folded into z by bcg_zfix_kernel before.
+template <class P>
+__global__ void __launch_bounds__(kBThreads, 4)
+bcg_pq_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P::V *__restrict__ diag,
+              const typename P::V *__restrict__ z, typename P::V *__restrict__ p, typename P::V *__restrict__ q,
+              BcgLayout L) {
+  using V = typename P::V;
+  const int count = L.head->acount;
+  for (int w = blockIdx.x; w < count; w += gridDim.x) {
+    const int c = L.alist[w];
+    const int inst = a.chunk_inst[c];
+    if (L.inst[inst].done) continue;
+    const bool first = L.inst[inst].refresh != 0;
+    const V beta = P::beta(L.inst[inst]);
+    typename P::Acc pq;
+    const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
+    for (int t = a.chunk_tile0[c]; t < t1; ++t) {
+      const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
+      const V zi = z[i];
+      const V w = P::fma(diag[i], zi, bsell_row<P>(i, a.n, a.slice_ptr, a.col, val, z));
+      const V pi = first ? zi : P::fma(beta, p[i], zi);
+      const V qi = first ? w : P::fma(beta, q[i], w);
+      p[i] = pi;
+      q[i] = qi;
+      pq.add(pi, qi);
+    }
+    const double v[1] = {bsum<kBThreads>(pq)};
+    double tot[1];
+    if (chunk_finish<1>(a, c, inst, v, L, tot) && threadIdx.x == 0) {
+      esr_bcg_inst &s = L.inst[inst];
+      s.pq = tot[0];
+      if (!(tot[0] != 0.0) || !isfinite(tot[0])) {
+        s.done = 3;  // breakdown
+        retire(L);
+      } else {
+        set_alpha(s, s.rz / tot[0]);
+      }
+    }
+  }
+}
+
+// ---- the same as two sweeps (FP64 policy): q = A p; p.q; alpha ...
 template <class P>
 __global__ void __launch_bounds__(kBThreads, 4)
 bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P::V *__restrict__ diag,
@@ -156,6 +209,55 @@ bcg_spmv_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P
       } else {
         set_alpha(s, s.rz / tot[0]);
       }
+    }
+  }
+}
+
+// ... and, at the end of the iteration, p = z + beta p (p = z for a first
+// direction: the GNN's fallback; init and replacement set p themselves)
+template <class P>
+__global__ void __launch_bounds__(kBThreads)
+bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V *__restrict__ p, BcgLayout L) {
+  using V = typename P::V;
+  const int count = L.head->acount;
+  for (int w = blockIdx.x; w < count; w += gridDim.x) {
+    const int c = L.alist[w];
+    const int inst = a.chunk_inst[c];
+    if (L.inst[inst].done) continue;
+    const bool first = L.inst[inst].refresh != 0;
+    const V beta = P::beta(L.inst[inst]);
+    const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
+    for (int t = a.chunk_tile0[c]; t < t1; ++t) {
+      const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
+      p[i] = first ? z[i] : P::fma(beta, p[i], z[i]);
+    }
+  }
+}
+
+// ---- GNN iterations, after the layers: the z the next direction uses.
+//   refresh == 1 (fallback to Jacobi; beta = 0): z = invdiag r
+//   GNN with a clipped correction (theta < 1): the layers stored
+//   z = zJ + zN; z = zJ + theta zN = theta z + (1 - theta) invdiag r
+template <class P>
+__global__ void __launch_bounds__(kBThreads)
+bcg_zfix_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const typename P::V *__restrict__ r,
+                typename P::V *__restrict__ z, BcgLayout L) {
+  using V = typename P::V;
+  const int count = L.head->acount;
+  for (int w = blockIdx.x; w < count; w += gridDim.x) {
+    const int c = L.alist[w];
+    const int inst = a.chunk_inst[c];
+    const esr_bcg_inst &st = L.inst[inst];
+    if (st.done) continue;
+    const bool refresh = st.refresh == 1;
+    if (!refresh && !(st.mode == kModeGnn && st.theta != 1.0)) continue;
+    const V th = P::of(st.theta), omth = P::of(1.0 - st.theta);
+    const int t1 = a.chunk_tile0[c + 1];
+    for (int t = a.chunk_tile0[c]; t < t1; ++t) {
+      const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
+      const V zj = invdiag ? P::mul(r[i], invdiag[i]) : r[i];
+      z[i] = refresh ? zj : P::fma(th, z[i], P::mul(omth, zj));
     }
   }
 }
@@ -231,43 +333,6 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
   }
 }
 
-// ---- update part 2: p = z + beta p
-// (refresh: the instance just fell back to Jacobi: p = invdiag r)
-template <class P>
-__global__ void __launch_bounds__(kBThreads)
-bcg_pupdate_kernel(BArgs a, const typename P::V *__restrict__ z, const typename P::V *__restrict__ r,
-                   const typename P::V *__restrict__ invdiag, typename P::V *__restrict__ p, BcgLayout L) {
-  using V = typename P::V;
-  const int count = L.head->acount;
-  for (int w = blockIdx.x; w < count; w += gridDim.x) {
-    const int c = L.alist[w];
-    const int inst = a.chunk_inst[c];
-    if (L.inst[inst].done) continue;
-    const V beta = P::beta(L.inst[inst]);
-    const bool refresh = L.inst[inst].refresh != 0;
-    const double theta = L.inst[inst].theta;
-    const bool blend = L.inst[inst].mode == kModeGnn && theta != 1.0;
-    V th = P::zero(), omth = P::zero();
-    if (blend) {
-      th = P::of(theta);
-      omth = P::of(1.0 - theta);
-    }
-    const int t1 = a.chunk_tile0[c + 1];
-#pragma unroll 2
-    for (int t = a.chunk_tile0[c]; t < t1; ++t) {
-      const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
-      if (refresh) {
-        p[i] = invdiag ? P::mul(r[i], invdiag[i]) : r[i];
-      } else if (blend) {  // z = (1 - theta) invdiag r + theta z_network
-        const V zb = P::fma(th, z[i], P::mul(omth, P::mul(r[i], invdiag[i])));
-        p[i] = P::fma(beta, p[i], zb);
-      } else {
-        p[i] = P::fma(beta, p[i], z[i]);
-      }
-    }
-  }
-}
-
 // ---- verification, pass 1: x64 = x for the instances to verify (its own
 // launch: the residual of a row reads x64 of other CTAs' rows)
 template <class P>
@@ -337,17 +402,26 @@ bcg_replace_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const dou
 
 template <class P>
 __global__ void __launch_bounds__(kBThreads)
-bcg_replace_p_kernel(BArgs a, const typename P::V *__restrict__ z, typename P::V *__restrict__ p, BcgLayout L) {
+bcg_replace_p_kernel(BArgs a, typename P::V *__restrict__ z, typename P::V *__restrict__ p, BcgLayout L) {
   const int inst = a.block_inst[blockIdx.x];
   esr_bcg_inst &st = L.inst[inst];
   if (st.verified != -2) return;
   const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
-  if (i < a.n) p[i] = P::fma(P::beta(st), p[i], z[i]);
+  // the continued direction p_new = z + beta p, in p (for bcg_spmv_kernel)
+  // and in z (for bcg_pq_kernel's first direction), so the next product is
+  // q = A p_new exactly (the update recomputes z from r before anything
+  // else reads it)
+  if (i < a.n) {
+    const typename P::V pn = P::fma(P::beta(st), p[i], z[i]);
+    p[i] = pn;
+    z[i] = pn;
+  }
   // the instance's tiles all pass the test above before any of them
   // re-arms it: the ticket counter orders them
   const double v[1] = {0.0};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
+    st.refresh = 2;
     st.verified = 0;
     st.restarts += 1;
     st.done = 0;
@@ -401,16 +475,21 @@ int run_iterate(const esr_batch *B, void *x, void *r, void *z, void *p, void *q,
   const BArgs a = bargs(B);
   bcg_compact_kernel<<<1, 1024, 0, s>>>(a, L);
   for (int32_t it = 0; it < k; ++it) {
-    bcg_spmv_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag, (const V *)p,
+    if constexpr (P::kFusedDirection)
+      bcg_pq_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag, (const V *)z, (V *)p,
                                                      (V *)q, L);
+    else
+      bcg_spmv_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag, (const V *)p,
+                                                       (V *)q, L);
     bcg_update_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->invdiag, (V *)x, (V *)r, (V *)z,
                                                        (const V *)p, (const V *)q, L);
     if (B->gnn) {
       const int st = esr::gnn_layers(B, r, q, z, ws, s);
       if (st) return st;
+      bcg_zfix_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->invdiag, (const V *)r, (V *)z, L);
     }
-    bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (const V *)r, (const V *)B->invdiag,
-                                                        (V *)p, L);
+    if constexpr (!P::kFusedDirection)
+      bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
   }
   ESR_LAUNCH_CHECK("esr_bcg_iterate");
   return ESR_OK;
@@ -425,7 +504,7 @@ int run_verify(const esr_batch *B, const double *b64, void *x, double *x64, doub
   bcg_export_kernel<P><<<B->nblocks, kBThreads, 0, s>>>(a, (const V *)x, x64, L);
   bcg_residual_kernel<<<B->nblocks, kBThreads, 0, s>>>(a, B->val64, B->diag64, b64, x64, r64, L);
   bcg_replace_kernel<P><<<B->nblocks, kBThreads, 0, s>>>(a, (const V *)B->invdiag, r64, (V *)r, (V *)z, L);
-  bcg_replace_p_kernel<P><<<B->nblocks, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
+  bcg_replace_p_kernel<P><<<B->nblocks, kBThreads, 0, s>>>(a, (V *)z, (V *)p, L);
   ESR_LAUNCH_CHECK("esr_bcg_verify");
   return ESR_OK;
 }

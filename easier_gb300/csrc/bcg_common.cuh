@@ -131,6 +131,10 @@ __device__ __forceinline__ double bsum(const DotAccDF &a) {
 struct PolF64 {
   using V = double;
   using Acc = DotAccD;
+  // FP64 iterations are bound by the FP64 pipe: the direction sweep of the
+  // double-float policy (q = A z + beta q, one more FMA a row) costs more
+  // than the separate p-update sweep it saves
+  static constexpr bool kFusedDirection = false;
   static __device__ __forceinline__ V alpha(const esr_bcg_inst &s) { return s.alpha; }
   static __device__ __forceinline__ V beta(const esr_bcg_inst &s) { return s.beta; }
   static __device__ __forceinline__ V neg(V a) { return -a; }
@@ -147,6 +151,7 @@ struct PolF64 {
 struct PolDF {
   using V = df64::df;
   using Acc = DotAccDF;
+  static constexpr bool kFusedDirection = true;
   static __device__ __forceinline__ V alpha(const esr_bcg_inst &s) { return V{s.alpha_df[0], s.alpha_df[1]}; }
   static __device__ __forceinline__ V beta(const esr_bcg_inst &s) { return V{s.beta_df[0], s.beta_df[1]}; }
   static __device__ __forceinline__ V neg(V a) { return df64::neg(a); }
@@ -160,12 +165,14 @@ struct PolDF {
   static __device__ __forceinline__ V off(float f) { return V{f, 0.f}; }
 };
 
-// sum over the row's SELL slots of val * x, in slot order
-template <class P>
-__device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
-                                                   const int32_t *__restrict__ col,
-                                                   const typename P::V *__restrict__ val,
-                                                   const typename P::V *__restrict__ x) {
+// sum over the row's SELL slots of val * x(col), in slot order; `x` maps a
+// column to its value (a vector load, or a value formed from several)
+// (WIDE: rows of <= 8 slots issue all their loads at once; otherwise, or for
+// a costly x, one slot after the other)
+template <class P, bool WIDE = true, class X>
+__device__ __forceinline__ typename P::V bsell_row_of(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
+                                                      const int32_t *__restrict__ col,
+                                                      const typename P::V *__restrict__ val, const X &x) {
   using V = typename P::V;
   const int64_t s = i >> 5;
   const int lane = (int)(i & 31);
@@ -174,7 +181,7 @@ __device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const i
   const int32_t *cp = col + b + lane;
   const V *vp = val + b + lane;
   V acc = P::zero();
-  if (w <= 8) {
+  if (WIDE && w <= 8) {
     int32_t c[8];
     V v[8], xc[8];
 #pragma unroll
@@ -186,7 +193,7 @@ __device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const i
     for (int k = 0; k < 8; ++k) {
       if (c[k] >= 0) {
         v[k] = vp[32 * k];
-        xc[k] = x[c[k]];
+        xc[k] = x(c[k]);
       }
     }
 #pragma unroll
@@ -196,9 +203,17 @@ __device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const i
   }
   for (int k = 0; k < w; ++k) {
     const int32_t c = __ldg(cp + 32 * k);
-    if (c >= 0 && (int64_t)c < n) acc = P::fma(vp[32 * k], x[c], acc);
+    if (c >= 0 && (int64_t)c < n) acc = P::fma(vp[32 * k], x(c), acc);
   }
   return acc;
+}
+
+template <class P>
+__device__ __forceinline__ typename P::V bsell_row(int64_t i, int64_t n, const int64_t *__restrict__ slice_ptr,
+                                                   const int32_t *__restrict__ col,
+                                                   const typename P::V *__restrict__ val,
+                                                   const typename P::V *__restrict__ x) {
+  return bsell_row_of<P>(i, n, slice_ptr, col, val, [x](int64_t j) { return x[j]; });
 }
 
 // FP64 row of the true residual

@@ -157,7 +157,8 @@ class BatchedPCG:
     """Lockstep (P)CG over a packed batch on one GPU.
 
     ``run`` enqueues iterations in groups of up to ``graph_iters``, each group
-    one CUDA graph (1 compaction + 3 persistent launches per iteration);
+    one CUDA graph (1 compaction + 2 persistent launches per iteration in
+    df64, 3 in FP64, 5 more with the GNN);
     between groups the host reads the 4-byte running-instance counter.
     The work shape -- 256-row tiles per CTA work unit (``tiles_per_chunk``)
     and persistent CTAs (``grid``) -- is set by ``autotune`` or by hand."""
@@ -246,9 +247,11 @@ class BatchedPCG:
 
     def bytes_per_row_iteration(self) -> float:
         """Algorithmic HBM bytes of one lockstep iteration per active packed
-        row (8-byte values in both precisions): SpMV streams col and val
-        (per stored slot), diag, gathers p, writes q; the update reads x, r,
-        p, q, invdiag and writes x, r, z; the p-update reads z, p, writes p."""
+        row (8-byte values in both precisions): the SpMV streams col and val
+        (per stored slot) and diag; 14 vector touches: df64 gathers z, reads
+        p, q and writes p, q (one sweep); FP64 gathers p and writes q, then
+        reads z, p and writes p (two sweeps); both then read x, r, p, q,
+        invdiag and write x, r, z."""
         slots = self.pack.slice_ptr[-1] / self.pack.n
         return slots * 12 + 8 * 14 + 8 / 32
 
@@ -271,7 +274,8 @@ class BatchedPCG:
                   _lib.ptr(self.p), _lib.ptr(self.q), int(k), _lib.ptr(self.ws), self._stream())
 
     def _group(self, k: int):
-        self.kernel_launches += 1 + (7 if self.gnn_desc is not None else 3) * k
+        per_it = (2 if self.precision == "df64" else 3) + (5 if self.gnn_desc is not None else 0)
+        self.kernel_launches += 1 + per_it * k
         if not self.use_graph:
             self._iterate_call(k)
             return

@@ -563,7 +563,8 @@ typedef struct {
   int32_t restarts;  /* residual replacements after a failed verification   */
   int32_t maxiter;
   int32_t mode;      /* 0 Jacobi, 1 GNN                                     */
-  int32_t refresh;   /* 1: next p-update restarts with p = invdiag r        */
+  int32_t refresh;   /* next direction: 1 restarts with p = invdiag r,       *
+                      * 2 keeps the p already set (q = A p)                 */
   int32_t fallbacks; /* GNN -> Jacobi switches                              */
   int32_t nrows;     /* rows before padding                                 */
   int32_t gnn_iters; /* iteration of the last GNN -> Jacobi switch (0 none) */
