@@ -494,3 +494,48 @@ def p1_edge_length(n: int, row: np.ndarray, col: np.ndarray) -> np.ndarray:
     di = (col % m) - (row % m)
     dj = (col // m) - (row // m)
     return np.sqrt((di * di + dj * dj).astype(np.float64))
+
+
+def main(argv: Optional[Sequence[str]] = None) -> None:
+    """Solve P1 Poisson systems on the batched engine and print one line per
+    solve: ``--grid N`` one constant-coefficient system (16-mode right hand
+    side, seed 0), else a seeded batch (``--count/--nmin/--nmax/--seed``);
+    ``--shape TILES,GRID`` fixes the work shape (default: autotune)."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(prog="python -m easier_gb300.numeric.batched")
+    ap.add_argument("--grid", type=int, default=None)
+    ap.add_argument("--count", type=int, default=16)
+    ap.add_argument("--nmin", type=int, default=32)
+    ap.add_argument("--nmax", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp64", "df64"], default="df64")
+    ap.add_argument("--shape", default=None)
+    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--repeat", type=int, default=2)
+    args = ap.parse_args(argv)
+    if args.grid:
+        s = mesh.p1_system(args.grid)
+        insts = [LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, mesh.random_mode_rhs(args.grid, 0))]
+    else:
+        insts = p1_instances(args.count, args.nmin, args.nmax, args.seed)
+    eng = BatchedPCG(insts, jacobi=True, precision=args.precision)
+    if args.shape:
+        t, g = (int(v) for v in args.shape.split(","))
+        eng.set_shape(t, g)
+    else:
+        eng.autotune()
+    for _ in range(args.repeat):
+        eng.reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = eng.solve(rtol=args.rtol)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ok = sum(r["status"] == "converged" for r in res)
+        print(f"{len(res)} systems, {ok} converged, {dt * 1e3:.1f} ms, max iterations {max(r['iters'] for r in res)}, "
+              f"replacements {sum(r['restarts'] for r in res)}, shape {eng.tiles_per_chunk},{eng.grid}", flush=True)
+
+
+if __name__ == "__main__":
+    main()
