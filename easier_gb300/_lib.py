@@ -141,7 +141,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 8
+ABI_VERSION = 9
 
 
 def library_path() -> Path:

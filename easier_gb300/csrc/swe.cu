@@ -24,7 +24,9 @@
 //          IEEE division) -> bitwise the reference's CPU backend.
 //   fast:  the same formulas with FMA contraction, one reciprocal of h_f per
 //          face for u_f = uh_f/h_f and v_f = vh_f/h_f, and a multiply by a
-//          precomputed 1/area.
+//          precomputed 1/area (the tiled kernel: face records whose sx, sy
+//          are already divided by the cell's area, the fluxes being linear
+//          in them).
 //
 // Stages (c1 = 0.5*dt, c3 = dt, c4 = dt/6, rounded to T like torch does):
 //   1: D1 = delta(s0);           S1 = s0 + c1*D1;  A = D1
@@ -310,7 +312,7 @@ constexpr int kTileMaxThreads = 1024;
 
 struct SlotsT {  // one tile's face slots, [3][n3] records {sx, sy, alpha, lnbr}
   const float4 *slot;
-  const float *area, *inv_area;
+  const float *area;  // exact arithmetic only (fast: sx, sy hold sx/area, sy/area)
   int n3, nL;
 };
 
@@ -318,11 +320,11 @@ struct SlotsT {  // one tile's face slots, [3][n3] records {sx, sy, alpha, lnbr}
 struct CellGeom {
   int32_t nb[3];
   float al[3], sx[3], sy[3];
-  float area, inv_area;
+  float area;
 };
 
-// The cell's geometry: three 16-byte face records and its area, all
-// loads issued together.
+// The cell's geometry: three 16-byte face records (and, exact, its area),
+// all loads issued together.
 template <bool EXACT>
 __device__ __forceinline__ void load_geom(int j, const SlotsT &g, CellGeom &c) {
 #pragma unroll
@@ -333,14 +335,58 @@ __device__ __forceinline__ void load_geom(int j, const SlotsT &g, CellGeom &c) {
     c.al[k] = f.z;
     c.nb[k] = __float_as_int(f.w);
   }
-  c.area = __ldg(g.area + j);
-  c.inv_area = EXACT ? 0.f : __ldg(g.inv_area + j);
+  c.area = EXACT ? __ldg(g.area + j) : 1.f;
 }
 
+// Stage state of a tile in shared memory.  Fast arithmetic: (h, uh) pairs
+// and vh, so a neighbour's state is two loads; exact: h, uh, vh arrays (the
+// paired layout costs the exact kernel registers and spills).
 template <bool EXACT>
-__device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, const float *hs, const float *us,
-                                           const float *vs, float &dh, float &du, float &dv) {
-  const float oh = hs[j], ou = us[j], ov = vs[j];
+struct TileState;
+
+template <>
+struct TileState<false> {
+  float2 *hu;
+  float *v;
+  // the layout's arrays over a shared buffer of `cells` entries at `base`
+  static __device__ __forceinline__ TileState at(float *smem, int total, int base) {
+    return TileState{reinterpret_cast<float2 *>(smem) + base, smem + 2 * total + base};
+  }
+  __device__ __forceinline__ void load(int j, float &h, float &u, float &w) const {
+    const float2 a = hu[j];
+    h = a.x;
+    u = a.y;
+    w = v[j];
+  }
+  __device__ __forceinline__ void store(int j, float h, float u, float w) const {
+    hu[j] = make_float2(h, u);
+    v[j] = w;
+  }
+};
+
+template <>
+struct TileState<true> {
+  float *h, *u, *v;
+  static __device__ __forceinline__ TileState at(float *smem, int total, int base) {
+    return TileState{smem + base, smem + total + base, smem + 2 * total + base};
+  }
+  __device__ __forceinline__ void load(int j, float &a, float &b, float &c) const {
+    a = h[j];
+    b = u[j];
+    c = v[j];
+  }
+  __device__ __forceinline__ void store(int j, float a, float b, float c) const {
+    h[j] = a;
+    u[j] = b;
+    v[j] = c;
+  }
+};
+
+template <bool EXACT>
+__device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, const TileState<EXACT> &s, float &dh,
+                                           float &du, float &dv) {
+  float oh, ou, ov;
+  s.load(j, oh, ou, ov);
   Acc3<float> acc{0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -350,26 +396,34 @@ __device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, con
         esr::raise_status(ESR_DEV_IDX_RANGE);
         continue;
       }
-      add_face<float, EXACT>(acc, oh, ou, ov, hs[q], us[q], vs[q], c.al[k], c.sx[k], c.sy[k]);
+      float nh, nu, nv;
+      s.load(q, nh, nu, nv);
+      add_face<float, EXACT>(acc, oh, ou, ov, nh, nu, nv, c.al[k], c.sx[k], c.sy[k]);
     } else if (q == -1) {
       add_wall<float, EXACT>(acc, oh, c.sx[k], c.sy[k]);
     }
   }
-  finish<float, EXACT>(acc, c.area, c.inv_area, dh, du, dv);
+  if (EXACT) {
+    finish<float, true>(acc, c.area, 0.f, dh, du, dv);
+  } else {  // the area is in the records
+    dh = -acc.Sh;
+    du = -(acc.Su + acc.Bu);
+    dv = -(acc.Sv + acc.Bv);
+  }
 }
 
 template <int STAGE, bool EXACT>
-__device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &cg, int nL, const float *hs,
-                                          const float *us, const float *vs, const float *h0, const float *u0,
-                                          const float *v0, float *ho, float *uo, float *vo,
+__device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &cg, int nL,
+                                          const TileState<EXACT> &in, const TileState<EXACT> &s0,
+                                          const TileState<EXACT> &out,
                                           float (&acc)[kTileOwnIters][3], float c, float4 *sout, int64_t cell_off) {
   using A = Ar<float, EXACT>;
   float dh, du, dv;
-  tile_delta<EXACT>(j, cg, nL, hs, us, vs, dh, du, dv);
+  tile_delta<EXACT>(j, cg, nL, in, dh, du, dv);
+  float h0, u0, v0;
+  s0.load(j, h0, u0, v0);
   if (STAGE < 4) {
-    ho[j] = A::madd(c, dh, h0[j]);
-    uo[j] = A::madd(c, du, u0[j]);
-    vo[j] = A::madd(c, dv, v0[j]);
+    out.store(j, A::madd(c, dh, h0), A::madd(c, du, u0), A::madd(c, dv, v0));
     if (r < kTileOwnIters && j < n0) {
       if (STAGE == 1) {
         acc[r][0] = dh;
@@ -383,9 +437,9 @@ __device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &
     }
   } else if (r < kTileOwnIters) {
     float4 o;
-    o.x = A::madd(c, A::add(acc[r][0], dh), h0[j]);
-    o.y = A::madd(c, A::add(acc[r][1], du), u0[j]);
-    o.z = A::madd(c, A::add(acc[r][2], dv), v0[j]);
+    o.x = A::madd(c, A::add(acc[r][0], dh), h0);
+    o.y = A::madd(c, A::add(acc[r][1], du), u0);
+    o.z = A::madd(c, A::add(acc[r][2], dv), v0);
     o.w = 0.f;
     sout[cell_off + j] = o;
   }
@@ -396,10 +450,9 @@ __device__ __forceinline__ void tile_cell(int r, int j, int n0, const CellGeom &
 // computed, so the group's loads are in flight together (the kernel is
 // latency-bound on these L1/L2 loads otherwise).
 template <int TT, int STAGE, bool EXACT>
-__device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, const float *hs, const float *us,
-                                           const float *vs, const float *h0, const float *u0, const float *v0,
-                                           float *ho, float *uo, float *vo, float (&acc)[kTileOwnIters][3],
-                                           float c, float4 *sout, int64_t cell_off) {
+__device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, const TileState<EXACT> &in,
+                                           const TileState<EXACT> &s0, const TileState<EXACT> &out,
+                                           float (&acc)[kTileOwnIters][3], float c, float4 *sout, int64_t cell_off) {
   constexpr int kIters = STAGE == 4 ? kTileOwnIters : kTileIters;
 #pragma unroll
   for (int r0 = 0; r0 < kIters; r0 += kTileGroup) {
@@ -413,8 +466,7 @@ __device__ __forceinline__ void tile_stage(int count, int n0, const SlotsT &g, c
     for (int u = 0; u < kTileGroup; ++u) {
       const int j = threadIdx.x + (r0 + u) * TT;
       if (r0 + u < kIters && j < count)
-        tile_cell<STAGE, EXACT>(r0 + u, j, n0, cg[u], g.nL, hs, us, vs, h0, u0, v0, ho, uo, vo, acc, c, sout,
-                                cell_off);
+        tile_cell<STAGE, EXACT>(r0 + u, j, n0, cg[u], g.nL, in, s0, out, acc, c, sout, cell_off);
     }
   }
 }
@@ -423,50 +475,49 @@ template <bool EXACT, int TT>
 __global__ void __launch_bounds__(TT, kTileMaxThreads / TT)
 swe_tile_step_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
-                     const float4 *__restrict__ gslot, const float *__restrict__ garea,
-                     const float *__restrict__ ginv_area, const float4 *__restrict__ sin,
+                     const float4 *__restrict__ gslot, const float *__restrict__ garea, const float4 *__restrict__ sin,
                      float4 *__restrict__ sout, int64_t nc, int max_local, int max_l3, float c1, float c3,
                      float c4) {
   extern __shared__ float smem[];
   const int t = blockIdx.x;
   const int32_t *mt = meta + 8 * (int64_t)t;
   const int cell_off = mt[0], n0 = mt[1], n1 = mt[2], n2 = mt[3], n3 = mt[4], nL = mt[5];
-  float *h0 = smem, *u0 = h0 + max_local, *v0 = u0 + max_local;
-  float *hA = v0 + max_local, *uA = hA + max_l3, *vA = uA + max_l3;
-  float *hB = vA + max_l3, *uB = hB + max_l3, *vB = uB + max_l3;
+  // s0 of the local list, then the two stage buffers of the level-<=3 cells
+  const int total = max_local + 2 * max_l3;
+  using TS = TileState<EXACT>;
+  const TS S0 = TS::at(smem, total, 0), SA = TS::at(smem, total, max_local),
+           SB = TS::at(smem, total, max_local + max_l3);
   const int64_t hb = offh[t];
   for (int j = threadIdx.x; j < nL; j += TT) {
     const int64_t gcell = j < n0 ? (int64_t)cell_off + j : (int64_t)__ldg(halo + hb + (j - n0));
     if (gcell < 0 || gcell >= nc) {  // corrupt layout: flag, never read out of bounds
       esr::raise_status(ESR_DEV_IDX_RANGE);
-      h0[j] = 1.f;
-      u0[j] = 0.f;
-      v0[j] = 0.f;
+      S0.store(j, 1.f, 0.f, 0.f);
       continue;
     }
     const float4 s = sin[gcell];
-    h0[j] = s.x;
-    u0[j] = s.y;
-    v0[j] = s.z;
+    S0.store(j, s.x, s.y, s.z);
   }
   __syncthreads();
   const int64_t o3 = off3[t];
-  const SlotsT g{gslot + 3 * o3, garea + o3, EXACT ? nullptr : ginv_area + o3, n3, nL};
+  const SlotsT g{gslot + 3 * o3, EXACT ? garea + o3 : nullptr, n3, nL};
   float acc[kTileOwnIters][3];
 #pragma unroll
   for (int r = 0; r < kTileOwnIters; ++r) acc[r][0] = acc[r][1] = acc[r][2] = 0.f;
-  tile_stage<TT, 1, EXACT>(n3, n0, g, h0, u0, v0, h0, u0, v0, hA, uA, vA, acc, c1, sout, cell_off);
+  tile_stage<TT, 1, EXACT>(n3, n0, g, S0, S0, SA, acc, c1, sout, cell_off);
   __syncthreads();
-  tile_stage<TT, 2, EXACT>(n2, n0, g, hA, uA, vA, h0, u0, v0, hB, uB, vB, acc, c1, sout, cell_off);
+  tile_stage<TT, 2, EXACT>(n2, n0, g, SA, S0, SB, acc, c1, sout, cell_off);
   __syncthreads();
-  tile_stage<TT, 3, EXACT>(n1, n0, g, hB, uB, vB, h0, u0, v0, hA, uA, vA, acc, c3, sout, cell_off);
+  tile_stage<TT, 3, EXACT>(n1, n0, g, SB, S0, SA, acc, c3, sout, cell_off);
   __syncthreads();
-  tile_stage<TT, 4, EXACT>(n0, n0, g, hA, uA, vA, h0, u0, v0, nullptr, nullptr, nullptr, acc, c4, sout, cell_off);
+  tile_stage<TT, 4, EXACT>(n0, n0, g, SA, S0, SA, acc, c4, sout, cell_off);
 }
 
 int64_t tile_smem_bytes(const esr_swe_tiles *T) {
   return (int64_t)(3 * (int64_t)T->max_local + 6 * (int64_t)T->max_l3) * (int64_t)sizeof(float);
 }
+// (3 floats a cell; the paired layout puts its float2 array first, so it is
+// 8-byte aligned at any max_local, max_l3)
 
 int check_tiles(const esr_swe_tiles *T) {
   if (!T) return esr::fail(ESR_ERR_ARG, "null tile layout");
@@ -480,7 +531,6 @@ int check_tiles(const esr_swe_tiles *T) {
   if (tile_smem_bytes(T) > 227 * 1024) return esr::fail(ESR_ERR_UNSUPPORTED, "tile needs more than 227 KB shared memory");
   if (!T->meta || !T->off3 || !T->offh || !T->slots || !T->area) return esr::fail(ESR_ERR_ARG, "null tile array");
   if (reinterpret_cast<uintptr_t>(T->slots) % 16 != 0) return esr::fail(ESR_ERR_ARG, "slots must be 16-byte aligned");
-  if (!T->exact && !T->inv_area) return esr::fail(ESR_ERR_ARG, "fast arithmetic needs inv_area");
   return ESR_OK;
 }
 
@@ -509,7 +559,7 @@ int run_tiles_tt(const esr_swe_tiles *tiles, double dt, void *state_a, void *sta
   for (int64_t k = 0; k < steps; ++k) {
     swe_tile_step_kernel<EXACT, TT><<<tiles->ntiles, TT, smem, s>>>(
         tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots,
-        (const float *)tiles->area, (const float *)tiles->inv_area, buf[k & 1], buf[(k + 1) & 1], tiles->nc,
+        (const float *)tiles->area, buf[k & 1], buf[(k + 1) & 1], tiles->nc,
         tiles->max_local, tiles->max_l3, c1, c3, c4);
   }
   ESR_LAUNCH_CHECK("esr_swe_tile_step");

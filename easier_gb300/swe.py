@@ -209,9 +209,13 @@ class SweEngine:
                                   _lib.ptr(self.inv_area), exact, 0)
         if self.tiled:
             src = self.tile_gsrc
-            # one 16-byte record per tile face slot: sx, sy, alpha, lnbr bits
-            self.t_slots = torch.stack([self.sx.reshape(-1)[src], self.sy.reshape(-1)[src],
-                                        self.alpha.reshape(-1)[src], self.tile_lnbr.view(torch.float32)],
+            # one 16-byte record per tile face slot: sx, sy, alpha, lnbr bits;
+            # fast arithmetic: sx / area, sy / area of the slot's cell
+            fx, fy = self.sx.reshape(-1)[src], self.sy.reshape(-1)[src]
+            if not exact:
+                inv = self.inv_area[src % self.nc]
+                fx, fy = fx * inv, fy * inv
+            self.t_slots = torch.stack([fx, fy, self.alpha.reshape(-1)[src], self.tile_lnbr.view(torch.float32)],
                                        dim=1).contiguous()
             self.t_area = self.area[self.tile_area_src].contiguous()
             self.t_inv_area = self.inv_area[self.tile_area_src].contiguous()

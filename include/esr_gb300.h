@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 8
+#define ESR_GB300_ABI_VERSION 9
 
 /* element types */
 enum {
@@ -265,7 +265,9 @@ int esr_swe_delta(const esr_swe_mesh *mesh, const void *state, void *delta,
  *   per local cell j < n3 and slot k: slots[3*off3[t] + k*n3 + j] = one
  *   16-byte record {float sx, float sy, float alpha, int32 lnbr} (lnbr =
  *   local index of the neighbour, -1 wall, -2 empty; one vector load per
- *   face), area[off3[t] + j].
+ *   face), area[off3[t] + j].  With exact == 0 the records hold sx / area
+ *   and sy / area of their cell (the fluxes are linear in sx, sy) and
+ *   area / inv_area are not read.
  * Limits: n0 <= 4096, n3 <= 6144, 12*nL + 24*n3 bytes <= 227 KB. */
 typedef struct {
   int64_t nc;
@@ -280,8 +282,8 @@ typedef struct {
   const int64_t *offh;
   const int32_t *halo;
   const void *slots;  /* 16-byte aligned face-slot records, see above */
-  const void *area;
-  const void *inv_area; /* [sum(n3)], used when exact == 0 */
+  const void *area;     /* [sum(n3)], read when exact != 0 */
+  const void *inv_area; /* not read (reserved) */
   int32_t exact;        /* as in esr_swe_mesh */
   int32_t pad2_;
 } esr_swe_tiles;
@@ -295,8 +297,8 @@ int64_t esr_swe_tile_smem_bytes(const esr_swe_tiles *tiles);
  * outside the limits. */
 int esr_swe_tile_threads(const esr_swe_tiles *tiles);
 
-/* `steps` steps of swe_main.py:121-141, one launch per step, bitwise equal
- * to esr_swe_step with the same `exact` setting.  Step k reads buffer k%2 and writes the other
+/* `steps` steps of swe_main.py:121-141, one launch per step; with exact != 0
+ * bitwise equal to esr_swe_step (exact), else within rounding of it.  Step k reads buffer k%2 and writes the other
  * ([nc][4] FP32 each, tile-major numbering): the result is in state_a when
  * `steps` is even, in state_b when odd. */
 int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
