@@ -86,9 +86,28 @@ struct Acc3 {
 // One interior face of a cell: flux terms of swe_main.py:87-117 added to the
 // cell's sums.  own/nb = (h, uh, vh) of the destination (this cell) and the
 // source (neighbour).
+//   exact: the reference's operations in its order;
+//   fast:  the same quantities regrouped, with F_h = uh_f sx + vh_f sy:
+//          phi_f = phi_src + alpha (phi_dst - phi_src)
+//          F_uh  = (uh_f / h_f) F_h + h_f^2 / 2 sx
+//          F_vh  = (vh_f / h_f) F_h + h_f^2 / 2 sy
+//          (u_f uh_f sx + u_f vh_f sy = u_f F_h), each term an FMA into the
+//          sum, and the wall terms go straight into the same sums.
 template <typename T, bool EXACT>
 __device__ __forceinline__ void add_face(Acc3<T> &s, T oh, T ou, T ov, T nh, T nu, T nv, T a, T fx, T fy) {
   using A = Ar<T, EXACT>;
+  if constexpr (!EXACT) {
+    const T hf = A::madd(a, A::sub(oh, nh), nh);
+    const T uhf = A::madd(a, A::sub(ou, nu), nu);
+    const T vhf = A::madd(a, A::sub(ov, nv), nv);
+    const T Fh = A::madd(uhf, fx, A::mul(vhf, fy));
+    const T Fi = A::mul(Fh, A::recip(hf));
+    const T hfs = A::mul(A::mul(T(0.5), hf), hf);
+    s.Sh = A::add(s.Sh, Fh);
+    s.Su = A::madd(uhf, Fi, A::madd(hfs, fx, s.Su));
+    s.Sv = A::madd(vhf, Fi, A::madd(hfs, fy, s.Sv));
+    return;
+  }
   const T half = T(0.5);
   const T om = A::sub(T(1), a);
   const T hf = A::madd(om, nh, A::mul(a, oh));   // (1 - alpha)*h[src] + alpha*h[dst]
@@ -113,8 +132,13 @@ template <typename T, bool EXACT>
 __device__ __forceinline__ void add_wall(Acc3<T> &s, T oh, T fx, T fy) {
   using A = Ar<T, EXACT>;
   const T gb = A::mul(T(0.5), A::mul(oh, oh));
-  s.Bu = A::madd(gb, fx, s.Bu);
-  s.Bv = A::madd(gb, fy, s.Bv);
+  if constexpr (EXACT) {
+    s.Bu = A::madd(gb, fx, s.Bu);
+    s.Bv = A::madd(gb, fy, s.Bv);
+  } else {
+    s.Su = A::madd(gb, fx, s.Su);
+    s.Sv = A::madd(gb, fy, s.Sv);
+  }
 }
 
 // delta = -(sums) / area
@@ -122,8 +146,13 @@ template <typename T, bool EXACT>
 __device__ __forceinline__ void finish(const Acc3<T> &s, T ar, T iar, T &dh, T &du, T &dv) {
   using A = Ar<T, EXACT>;
   dh = A::quot(-s.Sh, ar, iar);
-  du = A::quot(-A::add(s.Su, s.Bu), ar, iar);
-  dv = A::quot(-A::add(s.Sv, s.Bv), ar, iar);
+  if constexpr (EXACT) {
+    du = A::quot(-A::add(s.Su, s.Bu), ar, iar);
+    dv = A::quot(-A::add(s.Sv, s.Bv), ar, iar);
+  } else {  // wall terms are in Su, Sv
+    du = A::quot(-s.Su, ar, iar);
+    dv = A::quot(-s.Sv, ar, iar);
+  }
 }
 
 // ----------------------------------------------------------- staged --
@@ -405,10 +434,10 @@ __device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, con
   }
   if (EXACT) {
     finish<float, true>(acc, c.area, 0.f, dh, du, dv);
-  } else {  // the area is in the records
+  } else {  // the area is in the records, the wall terms in Su, Sv
     dh = -acc.Sh;
-    du = -(acc.Su + acc.Bu);
-    dv = -(acc.Sv + acc.Bv);
+    du = -acc.Su;
+    dv = -acc.Sv;
   }
 }
 
