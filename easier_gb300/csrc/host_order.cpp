@@ -305,7 +305,11 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
     }
     bfs(r.b, r.e, r.id, s);
     std::copy(order.begin(), order.end(), verts.begin() + r.b);
-    const int64_t half = r.b + sz / 2;
+    // the set ends as k = ceil(sz / max_part) parts: the first floor(k/2)
+    // parts' share of it goes left, so every final part has about sz / k
+    // vertices (not sz / 2^j: tiles come out close to max_part)
+    const int64_t k = (sz + max_part - 1) / max_part;
+    const int64_t half = r.b + sz * (k / 2) / k;
     const int64_t ida = next_id++, idb = next_id++;
     for (int64_t i = r.b; i < half; ++i) label[verts[i]] = ida;
     for (int64_t i = half; i < r.e; ++i) label[verts[i]] = idb;

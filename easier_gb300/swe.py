@@ -52,8 +52,9 @@ STATE = ("h", "uh", "vh")
 
 TILE_CELLS = 4096       # tile size cap (kernel limit: 4096 own cells)
 TILE_MIN_CELLS = 256
+TILE_TARGET = 3500      # large meshes: measured best at N=2000 (3,300-3,900 within 4%)
 # Target tile size; None = auto: one tile per SM while the mesh is small,
-# TILE_CELLS on large meshes.  Tiles of <= 1024 / 2048 own cells run 4 / 2
+# TILE_TARGET on large meshes.  Tiles of <= 1024 / 2048 own cells run 4 / 2
 # CTAs per SM.
 DEFAULT_TILE_CELLS: Optional[int] = None
 TILE_MAX_L3 = 6144      # kernel limit on tile + 3 halo rings
@@ -124,7 +125,7 @@ class SweEngine:
         """Largest tiles (least halo work) while there are enough of them to
         give every SM one."""
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count if self.device.type == "cuda" else 1
-        return max(TILE_MIN_CELLS, min(TILE_CELLS, -(-self.nc // sms)))
+        return max(TILE_MIN_CELLS, min(TILE_TARGET, -(-self.nc // sms)))
 
     # ----------------------------------------------------------- layout --
     def _build_layout(self) -> None:

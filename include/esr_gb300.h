@@ -305,8 +305,10 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
                       void *state_b, int64_t steps, void *stream);
 
 /* Host: partition an undirected graph (directed edge lists) into parts of at
- * most max_part vertices by recursive BFS bisection (compact, equal-sized
- * parts); part[v] in [0, *nparts).  No reference counterpart. */
+ * most max_part vertices by recursive BFS bisection (compact parts; a set
+ * due to end as k = ceil(size / max_part) parts is split floor(k/2) : ceil(k/2),
+ * so there are ceil(n / max_part) parts of nearly equal size for a
+ * connected graph); part[v] in [0, *nparts).  No reference counterpart. */
 int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src,
                          const int64_t *dst, int64_t max_part, int64_t *part,
                          int64_t *nparts);
