@@ -63,7 +63,12 @@ struct Ar<float, false> {
   static __device__ __forceinline__ float add(float a, float b) { return a + b; }
   static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
   static __device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
-  static __device__ __forceinline__ float recip(float y) { return __fdividef(1.0f, y); }
+  // approximate reciprocal (one MUFU op, ~1 ulp; flushes subnormals)
+  static __device__ __forceinline__ float recip(float y) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+    return r;
+  }
   static __device__ __forceinline__ float quot(float x, float, float yinv) { return x * yinv; }
 };
 
@@ -420,16 +425,14 @@ __device__ __forceinline__ void tile_delta(int j, const CellGeom &c, int nL, con
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int32_t q = c.nb[k];
-    if (q >= 0) {
-      if (q >= nL) {  // corrupt layout: flag, never read outside the tile's list
-        esr::raise_status(ESR_DEV_IDX_RANGE);
-        continue;
-      }
+    if ((uint32_t)q < (uint32_t)nL) {  // one compare: 0 <= q < nL
       float nh, nu, nv;
       s.load(q, nh, nu, nv);
       add_face<float, EXACT>(acc, oh, ou, ov, nh, nu, nv, c.al[k], c.sx[k], c.sy[k]);
     } else if (q == -1) {
       add_wall<float, EXACT>(acc, oh, c.sx[k], c.sy[k]);
+    } else if (q >= 0) {  // corrupt layout: flag, never read outside the tile's list
+      esr::raise_status(ESR_DEV_IDX_RANGE);
     }
   }
   if (EXACT) {
