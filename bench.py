@@ -329,13 +329,13 @@ def bench_swe(args, world, rank, local):
 
 
 def _ncu_traffic(kind, args):
-    """DRAM bytes per launch from the committed ncu summary, if any."""
+    """DRAM bytes per launch of this workload (kernel, dtype, mesh side) from
+    the committed ncu summary, if there is one."""
     f = ROOT / "profiles" / "traffic.json"
     if not f.exists():
         return None
     d = json.loads(f.read_text())
-    key = f"{kind}_{args.dtype}"
-    return d.get(key)
+    return d.get(f"{kind}_{args.dtype}_n{args.n}")
 
 
 # -------------------------------------------------------------- Poisson --
