@@ -246,3 +246,21 @@ def test_bisect_partition_balanced_and_deterministic():
     assert n1 == n2 and np.array_equal(p1, p2)
     sizes = np.bincount(p1)
     assert sizes.max() <= 1000 and sizes.min() >= 500
+
+
+def test_fast_record_order_sorts_each_cells_slots():
+    """The fast-arithmetic record order permutes only within a cell's three
+    slots and sorts them by local neighbour index."""
+    m = mesh.triangular_mesh(30)
+    lay = swe.cell_layout(m.nc, m.src, m.dst, m.bcells, tile_cells=500)
+    tl = swe.tile_layout(lay["nbr"], lay["part"])
+    order = swe._slots_by_neighbour(tl["meta"], tl["off3"], tl["lnbr"])
+    assert np.array_equal(np.sort(order), np.arange(order.size))
+    lnbr = tl["lnbr"]
+    for t in range(tl["meta"].shape[0]):
+        n3, base = int(tl["meta"][t, 4]), 3 * int(tl["off3"][t])
+        idx = base + np.arange(3 * n3).reshape(3, n3)
+        got = order[idx]
+        # same cell (column), ascending neighbours
+        assert np.array_equal(np.sort(got, axis=0), np.sort(idx, axis=0))
+        assert np.all(np.diff(lnbr[got], axis=0) >= 0)
