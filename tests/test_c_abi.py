@@ -48,3 +48,23 @@ def test_host_entry_points_from_c(c_program, tmp_path, n, max_part):
     part, k = mesh.bisect_partition(nc, m.src, m.dst, max_part)
     assert nparts == k and np.array_equal(load("part"), part)
     assert np.bincount(part).max() <= max_part
+
+
+@pytest.mark.gpu
+def test_device_entry_points_from_c(tmp_path):
+    """Selector gather + Reducer segment sum called from C99 on the caller's
+    stream: bitwise the host loops in the reference's edge order."""
+    import os
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cuda = os.environ.get("CUDA_HOME") or "/usr/local/cuda"
+    if cc is None or not (Path(cuda) / "include" / "cuda_runtime_api.h").exists():
+        pytest.skip("no C compiler or CUDA headers")
+    lib = _lib.library_path()
+    _lib.lib()
+    exe = tmp_path / "c_abi_device"
+    cmd = [cc, "-std=c99", "-Wall", "-Werror", "-I", str(HERE.parent / "include"), "-I", f"{cuda}/include",
+           str(HERE / "c_abi_device.c"), str(lib), f"-L{cuda}/lib64", "-lcudart", "-lm",
+           f"-Wl,-rpath,{lib.parent}", f"-Wl,-rpath,{cuda}/lib64", "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    res = subprocess.run([str(exe), "37"], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0 and res.stdout.strip() == "ok", res.stderr
