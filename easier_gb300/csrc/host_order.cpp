@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "esr_internal.h"
@@ -223,6 +224,93 @@ extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *p
 // compact (BFS slabs alternate direction as they shrink) and equal-sized
 // within one vertex.  Deterministic.  part[v] = part number; parts are
 // numbered in depth-first order of the recursion.
+namespace {
+
+// Recursive BFS bisection over disjoint ranges of `verts`.  A range's
+// vertices carry its label; ranges of one level touch disjoint vertices, so
+// subtrees run on separate threads: label is read across ranges (a
+// neighbour's) while its owner relabels it, hence relaxed atomic accesses
+// (the value read is never the reader's own id either way).  Labels are
+// heap-numbered (children of id: 2 id + 1, 2 id + 2) and BFS stamps are
+// 3 id + sweep, so no counter is shared; part ids come from each range's
+// first part and part count, in left-to-right order.
+struct Bisector {
+  const std::vector<int64_t> &ptr, &adj;
+  std::vector<int64_t> &label, &mark, &verts;
+  int64_t *part;
+  int64_t max_part;
+  int par_depth;
+
+  static int64_t ld(const int64_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
+  static void st(int64_t *p, int64_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
+
+  // BFS order of verts[b:e] (all labelled id) from start; unreached
+  // vertices (other components) are appended in their current order
+  void bfs(int64_t b, int64_t e, int64_t id, int64_t start, int64_t stamp, std::vector<int64_t> &order) const {
+    order.clear();
+    order.push_back(start);
+    mark[start] = stamp;
+    size_t h = 0;
+    while (true) {
+      while (h < order.size()) {
+        const int64_t v = order[h++];
+        for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+          const int64_t w = adj[k];
+          if (ld(&label[w]) == id && mark[w] != stamp) {
+            mark[w] = stamp;
+            order.push_back(w);
+          }
+        }
+      }
+      if ((int64_t)order.size() == e - b) break;
+      for (int64_t i = b; i < e; ++i)
+        if (mark[verts[i]] != stamp) {
+          mark[verts[i]] = stamp;
+          order.push_back(verts[i]);
+          break;
+        }
+    }
+  }
+
+  void run(int64_t b, int64_t e, int64_t id, int64_t first_part, int depth) {
+    const int64_t sz = e - b;
+    if (sz <= max_part) {
+      for (int64_t i = b; i < e; ++i) part[verts[i]] = first_part;
+      return;
+    }
+    // two sweeps find a vertex at a far end of the set (a pseudo-peripheral
+    // vertex); the BFS from there orders the set along its long axis, so the
+    // halves stay compact (one sweep leaves some long, thin parts)
+    std::vector<int64_t> order;
+    order.reserve(sz);
+    int64_t s = verts[b];
+    for (int sweep = 0; sweep < 2; ++sweep) {
+      bfs(b, e, id, s, 3 * id + sweep, order);
+      s = order.back();
+    }
+    bfs(b, e, id, s, 3 * id + 2, order);
+    std::copy(order.begin(), order.end(), verts.begin() + b);
+    // the set ends as k = ceil(sz / max_part) parts: the first floor(k/2)
+    // parts' share of it goes left, so every final part has about sz / k
+    // vertices (not sz / 2^j: tiles come out close to max_part)
+    const int64_t k = (sz + max_part - 1) / max_part;
+    const int64_t half = b + sz * (k / 2) / k;
+    const int64_t ida = 2 * id + 1, idb = 2 * id + 2;
+    for (int64_t i = b; i < half; ++i) st(&label[verts[i]], ida);
+    for (int64_t i = half; i < e; ++i) st(&label[verts[i]], idb);
+    if (depth < par_depth) {
+      std::thread left([&] { run(b, half, ida, first_part, depth + 1); });
+      run(half, e, idb, first_part + k / 2, depth + 1);
+      left.join();
+    } else {
+      run(b, half, ida, first_part, depth + 1);
+      run(half, e, idb, first_part + k / 2, depth + 1);
+    }
+  }
+};
+
+}  // namespace
+
 extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, const int64_t *dst,
                                     int64_t max_part, int64_t *part, int64_t *nparts) {
   if (n < 0 || m < 0 || max_part < 1) return esr::fail(ESR_ERR_ARG, "bad size");
@@ -246,77 +334,15 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
       adj[pos[dst[e]]++] = src[e];
     }
   }
-  // label[v] = id of the set v currently belongs to; BFS stays inside it
-  std::vector<int64_t> label(n, 0), mark(n, -1);
-  std::vector<int64_t> verts(n);
+  std::vector<int64_t> label(n, 0), mark(n, -1), verts(n);
   for (int64_t i = 0; i < n; ++i) verts[i] = i;
-  struct Range {
-    int64_t b, e, id;
-  };
-  std::vector<Range> stack;
-  stack.push_back({0, n, 0});
-  int64_t next_id = 1, out_parts = 0, stamp = 0;
-  std::vector<int64_t> order;
-  order.reserve(n);
-  auto bfs = [&](int64_t b, int64_t e, int64_t id, int64_t start) {
-    // BFS order of verts[b:e] (all with label id) from start; unreached
-    // vertices (other components) are appended in their current order
-    ++stamp;
-    order.clear();
-    order.push_back(start);
-    mark[start] = stamp;
-    size_t h = 0;
-    while (true) {
-      while (h < order.size()) {
-        int64_t v = order[h++];
-        for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
-          int64_t w = adj[k];
-          if (label[w] == id && mark[w] != stamp) {
-            mark[w] = stamp;
-            order.push_back(w);
-          }
-        }
-      }
-      if ((int64_t)order.size() == e - b) break;
-      for (int64_t i = b; i < e; ++i)
-        if (mark[verts[i]] != stamp) {
-          mark[verts[i]] = stamp;
-          order.push_back(verts[i]);
-          break;
-        }
-    }
-  };
-  while (!stack.empty()) {
-    Range r = stack.back();
-    stack.pop_back();
-    const int64_t sz = r.e - r.b;
-    if (sz <= max_part) {
-      for (int64_t i = r.b; i < r.e; ++i) part[verts[i]] = out_parts;
-      ++out_parts;
-      continue;
-    }
-    // two sweeps find a vertex at a far end of the set (a pseudo-peripheral
-    // vertex); the BFS from there orders the set along its long axis, so the
-    // halves stay compact (one sweep leaves some long, thin parts)
-    int64_t s = verts[r.b];
-    for (int sweep = 0; sweep < 2; ++sweep) {
-      bfs(r.b, r.e, r.id, s);
-      s = order.back();
-    }
-    bfs(r.b, r.e, r.id, s);
-    std::copy(order.begin(), order.end(), verts.begin() + r.b);
-    // the set ends as k = ceil(sz / max_part) parts: the first floor(k/2)
-    // parts' share of it goes left, so every final part has about sz / k
-    // vertices (not sz / 2^j: tiles come out close to max_part)
-    const int64_t k = (sz + max_part - 1) / max_part;
-    const int64_t half = r.b + sz * (k / 2) / k;
-    const int64_t ida = next_id++, idb = next_id++;
-    for (int64_t i = r.b; i < half; ++i) label[verts[i]] = ida;
-    for (int64_t i = half; i < r.e; ++i) label[verts[i]] = idb;
-    stack.push_back({half, r.e, idb});
-    stack.push_back({r.b, half, ida});
-  }
-  *nparts = out_parts;
+  // subtrees in parallel down to ~2 per hardware thread
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  int par_depth = 0;
+  while ((1u << par_depth) < 2 * hw && par_depth < 8) ++par_depth;
+  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth};
+  if (n > 0) bs.run(0, n, 0, 0, 0);
+  *nparts = n > 0 ? (n + max_part - 1) / max_part : 0;
   return ESR_OK;
 }
 
