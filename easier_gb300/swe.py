@@ -394,14 +394,17 @@ def _slots_by_neighbour(meta: np.ndarray, off3: np.ndarray, lnbr: np.ndarray) ->
     regular offsets: fewer shared-memory bank conflicts (modelled on the
     N=400 mesh: 4.1 -> 3.2 wavefronts per (h, uh) load of a warp)."""
     order = np.arange(lnbr.shape[0], dtype=np.int64)
-    for t in range(meta.shape[0]):
-        n3 = int(meta[t, 4])
-        if n3 == 0:
-            continue
-        base = 3 * int(off3[t])
-        idx = base + np.arange(3 * n3, dtype=np.int64).reshape(3, n3)
-        k = np.argsort(lnbr[idx], axis=0, kind="stable")
-        order[idx] = np.take_along_axis(idx, k, axis=0)
+    n3 = meta[:, 4].astype(np.int64)
+    total = int(n3.sum())
+    if total == 0:
+        return order
+    # every level-<=3 cell of every tile: its tile and local index j
+    tile = np.repeat(np.arange(n3.shape[0], dtype=np.int64), n3)
+    j = np.arange(total, dtype=np.int64) - np.repeat(np.cumsum(n3) - n3, n3)
+    # its three records: 3 * off3[t] + k * n3[t] + j
+    idx = 3 * off3.astype(np.int64)[tile] + np.arange(3, dtype=np.int64)[:, None] * n3[tile] + j
+    k = np.argsort(lnbr[idx], axis=0, kind="stable")
+    order[idx] = np.take_along_axis(idx, k, axis=0)
     return order
 
 
