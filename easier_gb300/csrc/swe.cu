@@ -331,8 +331,10 @@ int dispatch_delta(const esr_swe_mesh *m, const void *state, void *delta, cudaSt
 // runs all 4 stages there:
 //   stage 1 on cells of level <= 3 (reads s0 of levels <= 4)
 //   stage 2 on levels <= 2, stage 3 on levels <= 1, stage 4 on the tile.
-// Every cell value is computed with the operations of swe_stage_kernel, so
-// the result is bitwise the same for the same EXACT setting.  HBM traffic
+// In exact arithmetic every cell value is computed with the operations of
+// swe_stage_kernel, so the result is bitwise the same; in fast arithmetic
+// the face records carry sx/area, sy/area and a cell's faces are summed in
+// neighbour order (within rounding of the staged fast step).  HBM traffic
 // per step is the tile's geometry (plus the halo's), s0 of tile + halo, and
 // the new state; the stage states never leave the SM.
 // The CTA size TT is 1024, 512 or 256 threads with 1024 / TT CTAs per SM
