@@ -72,7 +72,11 @@ class PackedBatch:
     Slices never span instances (256-row blocks, 32-row slices), so each
     instance's SELL layout is built on its own and the layouts concatenated
     with row/slot offsets.  Entries of a row keep the reference's edge order
-    (stable sort of the Reducer index)."""
+    (stable sort of the Reducer index).  Without edge features, couplings
+    whose Ae is exactly 0 are left out: they add exactly nothing to a row's
+    sum of finite products (P1 grids: the hypotenuse couplings of right
+    triangles, a third of all), so the SpMV moves and multiplies less for
+    the same result.  The GNN's message passing keeps them as graph edges."""
 
     def __init__(self, instances: Sequence[LinsysInstance], edge_features: bool = False):
         if len(instances) == 0:
@@ -98,6 +102,10 @@ class PackedBatch:
             Ae, Av = _np(s.Ae, np.float64), _np(s.Av, np.float64)
             if row.shape != col.shape or row.shape != Ae.shape or Av.shape != (n,):
                 raise ValueError(f"instance {i}: inconsistent Linsys arrays")
+            if not edge_features:
+                keep = Ae != 0.0
+                if not keep.all():
+                    row, col, Ae = row[keep], col[keep], Ae[keep]
             rowptr, perm = mesh.csr_from_index(row, npad)
             slice_ptr, c, src_pos = mesh.sell_layout(npad, rowptr, perm, col, n)
             valid = src_pos >= 0
