@@ -101,3 +101,18 @@ def test_chunk_layout():
         # every chunk lies inside its instance's tiles
         assert np.all(ct0[:-1] >= ib0[ci]) and np.all(ct0[1:] <= ib0[ci + 1])
         assert np.array_equal(np.searchsorted(ic0, np.arange(len(ci)), side="right") - 1, ci)
+
+
+def test_pack_leaves_out_zero_couplings_but_the_gnn_graph_keeps_them():
+    """Exact-zero couplings (P1: the hypotenuse pairs) are not stored for the
+    SpMV, which still applies the same operator; the GNN's pack keeps them."""
+    rng = np.random.default_rng(1)
+    s = mesh.p1_system(12)
+    assert (s.Ae == 0).sum() > 0
+    inst = LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, rng.standard_normal(s.nunk),
+                          edge_len=np.ones(len(s.Ae)))
+    lean, full = PackedBatch([inst]), PackedBatch([inst], edge_features=True)
+    stored = lambda pk: int((pk.col >= 0).sum())  # noqa: E731
+    assert stored(lean) == int((s.Ae != 0).sum()) and stored(full) == len(s.Ae)
+    x = rng.standard_normal(lean.n)
+    assert np.array_equal(_sell_apply(lean, x), _sell_apply(full, x))
