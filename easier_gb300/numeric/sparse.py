@@ -54,13 +54,21 @@ class SellMatrix:
 
     @classmethod
     def from_linsys(cls, A, dtype: Optional[torch.dtype] = None) -> "SellMatrix":
+        """The Linsys's current values; couplings whose Ae is exactly 0 are
+        left out (they add exactly nothing to a row's sum of finite
+        products; the solvers rebuild their plan when Ae changes)."""
         sel, red = A.selector, A.reducer
         n = A.Av.shape[0]
         if red.n != n:
             raise ValueError(f"Linsys reducer has n={red.n} rows but Av has {n}")
         row = red.idx.detach().cpu().numpy().astype(np.int64)
         col = sel.idx.detach().cpu().numpy().astype(np.int64)
-        return cls.from_arrays(n, row, col, A.Ae.data, A.Av.data, dtype)
+        Ae = A.Ae.data
+        keep = (Ae != 0).cpu().numpy()
+        if not keep.all():
+            row, col = row[keep], col[keep]
+            Ae = Ae[torch.from_numpy(keep).to(Ae.device)]
+        return cls.from_arrays(n, row, col, Ae, A.Av.data, dtype)
 
     def astype(self, dtype: torch.dtype) -> "SellMatrix":
         return SellMatrix(self.n, self.slice_ptr, self.col, self.val.to(dtype), self.diag.to(dtype), self.src_pos)
