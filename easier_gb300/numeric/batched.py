@@ -439,7 +439,13 @@ class BatchedPCG:
         return [self._info(s) for s in self.instances()]
 
     def _free_graphs(self):
-        for h in getattr(self, "_one_graphs", {}).values():
+        graphs = getattr(self, "_one_graphs", {})
+        if graphs:
+            try:  # no launch of them may still be running
+                torch.cuda.current_stream(self.dev).synchronize()
+            except Exception:  # interpreter shutdown
+                pass
+        for h in graphs.values():
             try:
                 _lib.call("esr_bcg_graph_destroy", h)
             except Exception:  # interpreter shutdown
