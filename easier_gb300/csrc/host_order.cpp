@@ -101,10 +101,17 @@ extern "C" int esr_rcm_order(int64_t n, int64_t m, const int64_t *src,
   };
   for (int64_t i = 0; i < n; ++i) std::sort(adj.begin() + ptr[i], adj.begin() + ptr[i + 1], by_degree);
 
-  // candidate roots in (degree, index) order
+  // candidate roots in (degree, index) order: a counting sort by degree
+  // (stable, so equal degrees stay in index order)
   std::vector<int64_t> roots(n);
-  for (int64_t i = 0; i < n; ++i) roots[i] = i;
-  std::stable_sort(roots.begin(), roots.end(), by_degree);
+  {
+    int64_t maxd = 0;
+    for (int64_t i = 0; i < n; ++i) maxd = std::max(maxd, degree[i]);
+    std::vector<int64_t> start(maxd + 2, 0);
+    for (int64_t i = 0; i < n; ++i) start[degree[i] + 1]++;
+    for (int64_t d = 0; d <= maxd; ++d) start[d + 1] += start[d];
+    for (int64_t i = 0; i < n; ++i) roots[start[degree[i]]++] = i;
+  }
 
   std::vector<int64_t> level(n, -1);  // scratch for the peripheral search
   std::vector<int64_t> touched;
