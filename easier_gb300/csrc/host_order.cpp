@@ -2,8 +2,11 @@
 // index, and reverse Cuthill-McKee ordering.  All of it is exact integer
 // arithmetic and deterministic.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <string>
+#include <new>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -247,6 +250,7 @@ struct Bisector {
   int64_t *part;
   int64_t max_part;
   int par_depth;
+  std::atomic<bool> oom{false};  // a worker thread ran out of memory
 
   static int64_t ld(const int64_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
   static void st(int64_t *p, int64_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
@@ -305,10 +309,27 @@ struct Bisector {
     const int64_t ida = 2 * id + 1, idb = 2 * id + 2;
     for (int64_t i = b; i < half; ++i) st(&label[verts[i]], ida);
     for (int64_t i = half; i < e; ++i) st(&label[verts[i]], idb);
+    std::thread left;
     if (depth < par_depth) {
-      std::thread left([&] { run(b, half, ida, first_part, depth + 1); });
-      run(half, e, idb, first_part + k / 2, depth + 1);
+      try {
+        left = std::thread([&] {
+          try {
+            run(b, half, ida, first_part, depth + 1);
+          } catch (const std::bad_alloc &) {
+            oom.store(true);
+          }
+        });
+      } catch (const std::system_error &) {  // no thread to be had: this one does both halves
+      }
+    }
+    if (left.joinable()) {
+      try {
+        run(half, e, idb, first_part + k / 2, depth + 1);
+      } catch (const std::bad_alloc &) {
+        oom.store(true);
+      }
       left.join();
+      if (oom.load()) throw std::bad_alloc();
     } else {
       run(b, half, ida, first_part, depth + 1);
       run(half, e, idb, first_part + k / 2, depth + 1);
@@ -347,8 +368,12 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   int par_depth = 0;
   while ((1u << par_depth) < 2 * hw && par_depth < 8) ++par_depth;
-  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth};
-  if (n > 0) bs.run(0, n, 0, 0, 0);
+  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth, {}};
+  try {
+    if (n > 0) bs.run(0, n, 0, 0, 0);
+  } catch (const std::bad_alloc &) {
+    return esr::fail(ESR_ERR_ARG, "out of host memory");
+  }
   *nparts = n > 0 ? (n + max_part - 1) / max_part : 0;
   return ESR_OK;
 }
