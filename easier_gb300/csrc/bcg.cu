@@ -618,9 +618,14 @@ extern "C" int esr_bcg_graph_create(const esr_batch *B, const double *b64, const
     return esr::fail(ESR_ERR_ARG, "null argument");
   if (maxiter < 0 || maxiter > (1 << 26)) return esr::fail(ESR_ERR_ARG, "the one-launch graph needs a finite maxiter");
   if (k < 1 || k > 1024) return esr::fail(ESR_ERR_ARG, "iterations per body must be in [1, 1024]");
-  BcgGraph *G = new BcgGraph();
-  st = B->df64 ? build_graph<PolDF>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G)
-               : build_graph<PolF64>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G);
+  BcgGraph *G = new (std::nothrow) BcgGraph();
+  if (!G) return esr::fail(ESR_ERR_ARG, "out of host memory");
+  try {
+    st = B->df64 ? build_graph<PolDF>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G)
+                 : build_graph<PolF64>(B, b64, b, x, r, z, p, q, x64, r64, rtol, atol, maxiter, k, workspace, G);
+  } catch (const std::bad_alloc &) {
+    st = esr::fail(ESR_ERR_ARG, "out of host memory");
+  }
   if (st) {
     destroy_graph(G);
     return st;

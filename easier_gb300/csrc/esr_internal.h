@@ -3,6 +3,8 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <exception>
+#include <new>
 #include <string>
 
 #include "../../include/esr_gb300.h"
@@ -13,6 +15,19 @@ namespace esr {
 int fail(int code, const std::string &msg);
 
 }  // namespace esr
+
+// Body guard of the host-side extern "C" entry points: a C++ exception
+// (host memory exhausted, a thread that cannot be created) becomes an
+// error status instead of crossing the C boundary.
+#define ESR_HOST_TRY try {
+#define ESR_HOST_CATCH                                                        \
+  }                                                                           \
+  catch (const std::bad_alloc &) {                                            \
+    return esr::fail(ESR_ERR_ARG, "out of host memory");                      \
+  }                                                                           \
+  catch (const std::exception &ex) {                                          \
+    return esr::fail(ESR_ERR_ARG, std::string("host error: ") + ex.what()); \
+  }
 
 #ifdef __CUDACC__
 #include <cuda_runtime.h>

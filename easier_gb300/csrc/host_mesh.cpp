@@ -121,6 +121,7 @@ extern "C" int esr_mesh_sizes(int64_t n, int64_t *nc, int64_t *ne,
 extern "C" int esr_mesh_triangular(int64_t n, int64_t *src, int64_t *dst,
                                    int64_t *cells, int64_t *bcells,
                                    int64_t *bpoints, double *points) {
+  ESR_HOST_TRY
   int64_t nc, ne, nbc, np;
   int st = esr_mesh_sizes(n, &nc, &ne, &nbc, &np);
   if (st) return st;
@@ -213,6 +214,7 @@ extern "C" int esr_mesh_triangular(int64_t n, int64_t *src, int64_t *dst,
     }
   }
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 static int check_mesh_args(int64_t nc, int64_t ne, int64_t nbc, const int64_t *src,
@@ -237,6 +239,7 @@ extern "C" int esr_swe_geometry(int64_t nc, int64_t ne, int64_t nbc,
                                 double *sx, double *sy, double *alpha,
                                 double *area, double *x, double *y,
                                 double *bsx, double *bsy) {
+  ESR_HOST_TRY
   int st = check_mesh_args(nc, ne, nbc, src, dst, cells, bcells, bpoints, points);
   if (st) return st;
   // per cell: centroid and area (assemble_shallow_water.py:225-240)
@@ -274,6 +277,7 @@ extern "C" int esr_swe_geometry(int64_t nc, int64_t ne, int64_t nbc,
     bsy[b] = -bn.y;
   }
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 extern "C" int esr_poisson_fv_assemble(int64_t nc, int64_t ne, int64_t nbc,
@@ -284,6 +288,7 @@ extern "C" int esr_poisson_fv_assemble(int64_t nc, int64_t ne, int64_t nbc,
                                        const double *points, double *Af,
                                        double *Ac, double *b, double *rho,
                                        double *centroid) {
+  ESR_HOST_TRY
   int st = check_mesh_args(nc, ne, nbc, src, dst, cells, bcells, bpoints, points);
   if (st) return st;
   std::vector<Pt> cent(nc);
@@ -345,6 +350,7 @@ extern "C" int esr_poisson_fv_assemble(int64_t nc, int64_t ne, int64_t nbc,
   for (int64_t c = 0; c < nc; ++c) Ac[c] = Ac[c] - bacc[c];
   (void)hit;
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 // ---------------------------------------------------------------------------
@@ -365,6 +371,7 @@ extern "C" int esr_p1_sizes(int64_t n, int64_t *nunk, int64_t *nnz_off) {
 
 extern "C" int esr_p1_assemble(int64_t n, const double *kappa, int64_t *row,
                                int64_t *col, double *Ae, double *Av) {
+  ESR_HOST_TRY
   int64_t nunk, nnz;
   int st = esr_p1_sizes(n, &nunk, &nnz);
   if (st) return st;
@@ -433,4 +440,5 @@ extern "C" int esr_p1_assemble(int64_t n, const double *kappa, int64_t *row,
   }
   if (k != nnz) return esr::fail(ESR_ERR_ARG, "P1 assembly count mismatch");
   return ESR_OK;
+  ESR_HOST_CATCH
 }

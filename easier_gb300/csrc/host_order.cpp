@@ -32,6 +32,7 @@ extern "C" int esr_abi_version(void) { return ESR_GB300_ABI_VERSION; }
 // zipsort of passes/utils.py:301-336), plus the CSR row pointer.
 extern "C" int esr_csr_from_index(const int64_t *idx, int64_t m, int64_t n,
                                   int64_t *rowptr, int64_t *perm) {
+  ESR_HOST_TRY
   if (m < 0 || n < 0) return esr::fail(ESR_ERR_ARG, "negative size");
   if (!rowptr || (m && (!idx || !perm))) return esr::fail(ESR_ERR_ARG, "null pointer");
   std::fill(rowptr, rowptr + n + 1, 0);
@@ -47,6 +48,7 @@ extern "C" int esr_csr_from_index(const int64_t *idx, int64_t m, int64_t n,
   std::vector<int64_t> fill(rowptr, rowptr + n);
   for (int64_t k = 0; k < m; ++k) perm[fill[idx[k]]++] = k;
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 // Reverse Cuthill-McKee.
@@ -59,6 +61,7 @@ extern "C" int esr_csr_from_index(const int64_t *idx, int64_t m, int64_t n,
 //  3. Reverse the concatenated order.
 extern "C" int esr_rcm_order(int64_t n, int64_t m, const int64_t *src,
                              const int64_t *dst, int64_t *order) {
+  ESR_HOST_TRY
   if (n < 0 || m < 0) return esr::fail(ESR_ERR_ARG, "negative size");
   if (!order || (m && (!src || !dst))) return esr::fail(ESR_ERR_ARG, "null pointer");
   if (n == 0) return ESR_OK;
@@ -182,6 +185,7 @@ extern "C" int esr_rcm_order(int64_t n, int64_t m, const int64_t *src,
   }
   std::reverse(order, order + n);
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 // SELL-32 layout of a Linsys.  Slices of 32 consecutive rows; a slice is as
@@ -191,6 +195,7 @@ extern "C" int esr_rcm_order(int64_t n, int64_t m, const int64_t *src,
 extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *perm,
                               const int64_t *colidx, int64_t ncols, int64_t *slice_ptr,
                               int32_t *col, int64_t *src_pos) {
+  ESR_HOST_TRY
   if (n < 0 || ncols < 0) return esr::fail(ESR_ERR_ARG, "negative size");
   if (!rowptr || !slice_ptr) return esr::fail(ESR_ERR_ARG, "null pointer");
   if (ncols > ((int64_t)1 << 31) - 1) return esr::fail(ESR_ERR_UNSUPPORTED, "more than 2^31-1 columns");
@@ -226,6 +231,7 @@ extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *p
     }
   }
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 // Recursive BFS bisection: split a vertex set in two by the first half of a
@@ -390,6 +396,7 @@ extern "C" int esr_swe_tile_layout(int64_t nc, const int32_t *nbr, const int64_t
                                    int32_t *meta, int64_t *total_halo, int64_t *total_l3, int64_t *off3,
                                    int64_t *offh, int32_t *halo, int32_t *lnbr, int64_t *slot_src,
                                    int64_t *area_src) {
+  ESR_HOST_TRY
   if (nc <= 0 || ntiles <= 0) return esr::fail(ESR_ERR_ARG, "empty layout");
   if (!nbr || !part || !meta || !total_halo || !total_l3) return esr::fail(ESR_ERR_ARG, "null pointer");
   const bool fill = halo != nullptr;
@@ -468,4 +475,5 @@ extern "C" int esr_swe_tile_layout(int64_t nc, const int32_t *nbr, const int64_t
   *total_halo = tot_h;
   *total_l3 = tot_3;
   return ESR_OK;
+  ESR_HOST_CATCH
 }
