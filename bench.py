@@ -127,6 +127,44 @@ def _max_over_ranks(world, v: float) -> float:
     return float(t.item())
 
 
+# ------------------------------------------------- workload configuration --
+# Both arms (ours and --impl reference) print the same config dict for the
+# same arguments: it names the workload only, never a result.
+def swe_sizes(n):
+    """Cells, directed interior edges and wall faces of the tutorial mesh
+    (4 triangles per grid square)."""
+    return 4 * n * n, 12 * n * n - 4 * n, 4 * n
+
+
+def swe_config(args, world):
+    nc, ne, nbc = swe_sizes(args.n)
+    s = 4 if args.dtype == "f32" else 8
+    resident = nc * (16 + 3 * 16 + 4) + ne * 4
+    return {"workload": f"shallow water, tutorial mesh N={args.n} ({nc} cells, {ne} directed edges), dt={args.dt}",
+            "cells": nc, "edges": ne, "dt": args.dt, "dtype": args.dtype, "precision": args.precision,
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (state + geometry ~%.2f GB resident)" % (resident * s / 4 / 1e9)}
+
+
+def poisson_config(args, world):
+    return {"workload": f"P1 Poisson {args.n}x{args.n} grid, 16 random sine modes (seed 0), Jacobi-PCG to FP64 "
+                        f"true rel. residual 1e-8",
+            "unknowns": (args.n - 1) ** 2, "precision": args.precision, "parallelism": f"replicas x{world}",
+            "l2": "working set larger than L2 (matrix + 6 vectors)"}
+
+
+def batched_config(args, world):
+    from easier_gb300.numeric.batched import p1_sides
+    sides = p1_sides(args.count, args.nmin, args.nmax, seed=args.seed)
+    what = "GNN-preconditioned flexible CG vs Jacobi-PCG" if args.workload == "gnn" else "Jacobi-PCG"
+    return {"workload": f"batched P1 Poisson, {args.count} instances (seed {args.seed}), N ~ U{{{args.nmin}.."
+                        f"{args.nmax}}}, GRF kappa (corr. 0.1, var 1), {what} per instance to FP64 true rel. "
+                        f"residual 1e-8",
+            "instances": args.count, "unknowns": int(((sides - 1) ** 2).sum()), "seed": args.seed,
+            "precision": "fp64" if args.workload != "gnn" and args.precision == "fp64" else "df64",
+            "parallelism": f"replicas x{world}", "l2": "working set larger than L2 (vectors alone > 1 GB)"}
+
+
 # ------------------------------------------------------------------ SWE --
 def swe_algorithmic_bytes(nc, ne, nbc, s):
     """Bytes of one time step under the per-delta byte model: per delta
@@ -259,7 +297,7 @@ def bench_swe(args, world, rank, local):
     lps = eng.launches_per_step()
     peak, peak_kind = _peaks()
     achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
-    secondary = swe_secondary(args, eng, dev, stream) if args.dtype == "f32" else None
+    secondary = swe_secondary(args, eng, dev, stream) if args.dtype == "f32" else {}
 
     # end to end through the C ABI with host buffers: every step uploads the
     # state (h, uh, vh per cell: 12 bytes, the 4th lane of the device layout
@@ -301,40 +339,45 @@ def bench_swe(args, world, rank, local):
         cpu = {"value": v, "unit": "cell-steps/s", "cores": thr, "kind": "port",
                "sample": f"{args.cpu_steps} oracle steps (torch CPU ops, reference op order) at N={args.n}, "
                          f"{args.dtype}, {wall:.1f} s"}
-    traffic = _ncu_traffic("swe_tiled" if eng.tiled else "swe", args)
+    traffic = _ncu_traffic(eng.traffic_key() if eng.tiled else "swe", args)
+    step_s = ms / args.steps / 1e3
+    kernel_bytes = touched / lps  # what one launch of the fused kernel must move, each array once
     line = {
         "metric": "SWE cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
         "data": "synthetic (tutorial mesh generator, centred Gaussian bump, uh=vh=0)",
-        "config": {"workload": f"shallow water, tutorial mesh N={args.n} ({nc} cells, {eng.b['ne']} directed edges), "
-                               f"RCM + destination-ordered face slots, dt={args.dt}",
-                   "cells": nc, "edges": eng.b["ne"], "dt": args.dt, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (state+geometry ~%.2f GB)" % (bytes_step / 4 / 1e9)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic,
+        "config": swe_config(args, world),
+        "roofline": {"bound": "hbm", "achieved": kernel_bytes / (step_s / lps) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": kernel_bytes / (step_s / lps) / 1e9 / peak, "peak_kind": peak_kind,
+                     "traffic": traffic,
                      "kernel": ("swe_tile_step_kernel (1 launch per step)" if eng.tiled else
                                 "swe_stage_kernel (4 launches per step; bytes and time per step / 4)"),
-                     "algorithmic_bytes_per_launch": bytes_step / lps,
-                     "model": "per-step byte model of the unfused step: four delta passes (edge geometry, "
-                              "state, area, rowptr, delta out) and the stage combination through HBM; the "
-                              "fused kernel keeps the stage states on chip, so frac > 1 measures the fusion",
-                     "touched_bytes_per_launch": touched / lps,
-                     "touched_frac": touched / (ms / args.steps / 1e3) / 1e9 / peak,
-                     "dram_frac": (traffic / (ms / args.steps / 1e3) / 1e9 / peak) if traffic else None},
-        "precision": args.precision,
-        "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
-                   "within 1e-5 (FP32) / 1e-10 (FP64) relative of the reference FP64 run after 1,000 steps"),
-        "secondary": secondary,
+                     "algorithmic_bytes_per_launch": kernel_bytes,
+                     "bytes_model": eng.bytes_model(),
+                     "dram_frac": (traffic / (step_s / lps) / 1e9 / peak) if traffic else None,
+                     "contract_model_bytes_per_step": bytes_step,
+                     "contract_model_frac": achieved / peak,
+                     "contract_model": "the unfused step's bytes (four delta passes and the stage combination "
+                                       "through HBM): not what the fused kernel moves, so not an HBM fraction"},
         "engine": eng.describe(),
+        "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
+                   "state within 1e-5 (FP32) relative max-norm of the FP64 oracle (N=100 x 1,000 steps, N=2000 x 5 "
+                   "steps)"),
+        "secondary": secondary,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": lps * args.steps, "clocks": clk.summary(),
     }
+    if not args.no_solvers:
+        del eqn, eng, host, stage, a, b
+        torch.cuda.empty_cache()
+        line["secondary"]["solvers"] = solver_secondaries(args, world, rank, local)
     return line
 
 
 def _ncu_traffic(kind, args):
-    """DRAM bytes per launch of this workload (kernel, dtype, mesh side) from
-    the committed ncu summary, if there is one."""
+    """DRAM bytes per launch of this kernel variant on this mesh (ncu
+    dram__bytes_read.sum + dram__bytes_write.sum of one launch), from the
+    committed profile summary, if there is one."""
     f = ROOT / "profiles" / "traffic.json"
     if not f.exists():
         return None
@@ -392,13 +435,13 @@ def bench_poisson(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": dtype,
         "data": "synthetic (16 random sine modes, seed 0)",
-        "config": {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to FP64 true rel. residual 1e-8",
-                   "unknowns": eqn.nunk, "couplings": int(eqn.selector.idx.numel()), "iterations": nit,
-                   "precision": args.precision, "bytes_per_iteration": bytes_it,
-                   "replacements": info.get("restarts", info.get("replacements")),
-                   "true_rel_residual": rel, "parallelism": f"replicas x{world}"},
+        "config": poisson_config(args, world),
+        "solve": {"couplings": int(eqn.selector.idx.numel()), "iterations": nit, "bytes_per_iteration": bytes_it,
+                  "replacements": info.get("restarts", info.get("replacements")), "true_rel_residual": rel},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None},
+                     "peak_kind": peak_kind, "traffic": None,
+                     "bytes_model": "per iteration: SpMV col + value per stored slot and the diagonal, 14 vector "
+                                    "touches of 8 bytes per row (x iterations of the solve)"},
         "gpu_launches": int(getattr(eng, "kernel_launches", 0) - launches0),
         "clocks": clk.summary(),
     }
@@ -546,19 +589,17 @@ def bench_batched(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == "fp64" else "df64 (f32 pairs)",
         "data": f"synthetic (seed {args.seed}: GRF kappa corr. 0.1 var 1, 16 random sine modes)",
-        "config": {"workload": f"batched P1 Poisson, {pk.ninst} instances, N ~ U{{{args.nmin}..{args.nmax}}}, "
-                               f"Jacobi-PCG per instance to FP64 true rel. residual 1e-8",
-                   "unknowns": int(pk.sizes.sum()), "packed_rows": pk.n, "stored_slots": int(pk.slice_ptr[-1]),
-                   "iterations_max": max(iters), "iterations_mean": float(np.mean(iters)),
-                   "restarts": int(sum(r["restarts"] for r in res)), "precision": prec,
-                   "graph_iters": eng.graph_iters, "tiles_per_chunk": eng.tiles_per_chunk, "grid": eng.grid,
-                   "launch": ("host-polled CUDA graphs of graph_iters iterations" if args.polled else
-                              "one CUDA graph launch per batch solve (device-side while loop)"),
-                   "autotune": None if tuning is None else
-                   {"s": tune_s, "ms_per_iter_all_running": tuning["ms_per_iter"],
-                    "candidates": len(tuning["table"])},
-                   "setup_s": prep, "inputs_vs_l2": "working set > L2 (vectors alone > 1 GB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": batched_config(args, world),
+        "solve": {"packed_rows": pk.n, "stored_slots": int(pk.slice_ptr[-1]),
+                  "iterations_max": max(iters), "iterations_mean": float(np.mean(iters)),
+                  "restarts": int(sum(r["restarts"] for r in res)),
+                  "graph_iters": eng.graph_iters, "tiles_per_chunk": eng.tiles_per_chunk, "grid": eng.grid,
+                  "launch": ("host-polled CUDA graphs of graph_iters iterations" if args.polled else
+                             "one CUDA graph launch per batch solve (device-side while loop)"),
+                  "autotune": None if tuning is None else
+                  {"s": tune_s, "ms_per_iter_all_running": tuning["ms_per_iter"],
+                   "candidates": len(tuning["table"])},
+                  "setup_s": prep},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None,
                      "bytes_per_row_iteration": eng.bytes_per_row_iteration()},
@@ -575,6 +616,14 @@ def bench_batched(args, world, rank, local):
 
 
 # ---------------------------------------------------- GNN-preconditioned --
+def gnn_row_bytes(slots_per_row: float) -> float:
+    """Algorithmic bytes of one GNN application per packed row: 4 layers
+    each reading and writing the row's 32 BF16 features (64 + 64 bytes) and
+    each stored slot's column index and edge inputs (4 + 8 bytes), plus the
+    residual, kappa input and output (20 bytes)."""
+    return 4 * (128 + 12 * slots_per_row) + 20
+
+
 def bench_gnn(args, world, rank, local):
     """Flexible CG with the GNN preconditioner against Jacobi-PCG, both
     batched and df64, on held-out seeded instances."""
@@ -611,7 +660,18 @@ def bench_gnn(args, world, rank, local):
         if bad:
             raise RuntimeError(f"{name}: {len(bad)} instances not FP64-verified at 1e-8, e.g. {bad[0]}")
         its = np.array([r["iters"] for r in res])
-        out[name] = {"solves_per_s": world * len(insts) / (ms / args.steps / 1e3), "ms_per_batch": ms / args.steps,
+        # algorithmic bytes: the CG iterations (engine byte model per packed
+        # row) plus, per GNN application, GNN_ROW_BYTES per packed row
+        npad = np.diff(eng.pack.inst_block0.astype(np.int64)) * 256
+        slots = eng.pack.slice_ptr[-1] / eng.pack.n
+        cg_bytes = float(sum((r["iters"] + 1 + r["restarts"]) * n for r, n in zip(res, npad)))
+        cg_bytes *= eng.bytes_per_row_iteration()
+        gnn_apps = float(sum(r["fallback_iter"] * n for r, n in zip(res, npad))) if name == "gnn" else 0.0
+        gnn_bytes = gnn_apps * gnn_row_bytes(slots)
+        sec = ms / args.steps / 1e3
+        out[name] = {"solves_per_s": world * len(insts) / sec, "ms_per_batch": ms / args.steps,
+                     "bytes_per_solve_batch": cg_bytes + gnn_bytes,
+                     "achieved_gbs": (cg_bytes + gnn_bytes) / sec / 1e9,
                      "iters_mean": float(its.mean()), "iters_max": int(its.max()),
                      "fallbacks": int(sum(r["fallbacks"] for r in res)),
                      "theta_clips": int(sum(r["clips"] for r in res)),
@@ -626,17 +686,51 @@ def bench_gnn(args, world, rank, local):
         "ms_per_step": g["ms_per_batch"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "df64 (f32 pairs) CG, bf16 GNN with f32 accumulation",
         "data": f"synthetic held-out instances (seed {args.seed}); weights {WEIGHTS_FILE.name}",
-        "config": {"workload": f"{len(insts)} P1 Poisson instances, N ~ U{{{args.nmin}..{args.nmax}}}, GRF kappa, "
-                               f"to FP64-verified rel. residual 1e-8",
-                   "gnn": {k: v for k, v in g.items() if k != "clocks"},
-                   "jacobi": {k: v for k, v in j.items() if k != "clocks"},
-                   "gnn_over_jacobi_solves_per_s": g["solves_per_s"] / j["solves_per_s"],
-                   "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
-                     "peak_kind": peak_kind, "traffic": None},
+        "config": batched_config(args, world),
+        "solve": {"gnn": {k: v for k, v in g.items() if k != "clocks"},
+                  "jacobi": {k: v for k, v in j.items() if k != "clocks"},
+                  "gnn_over_jacobi_solves_per_s": g["solves_per_s"] / j["solves_per_s"]},
+        "roofline": {"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": g["achieved_gbs"] / peak, "peak_kind": peak_kind, "traffic": None,
+                     "bytes_model": "df64 CG bytes per packed row-iteration (engine model) plus, per GNN "
+                                    "application, 4 layers x (BF16 features in and out, 64 + 64 bytes, and 12 "
+                                    "bytes per stored slot) + 20 bytes of inputs and output per packed row"},
         "gpu_launches": g["launches"],
         "clocks": g["clocks"],
     }
+
+
+# ------------------------------------------- solver figures beside SWE --
+def solver_secondaries(args, world, rank, local):
+    """The solver workloads, each bounded, on the default SWE line:
+    P1-1000 Jacobi-PCG in FP64 and double-float (3 timed solves each), the
+    256-instance batch in double-float (one timed one-launch batch solve)
+    and GNN flexible CG against Jacobi-PCG on the held-out batch (one timed
+    batch each).  Each keeps its own CUDA-event timing, FP64-verified
+    residuals, roofline and clock record."""
+    import copy
+    out = {}
+    runs = (("poisson_p1_1000_fp64", bench_poisson, dict(workload="poisson", n=1000, precision="native", steps=3,
+                                                          warmup=1, seed=0)),
+            ("poisson_p1_1000_df64", bench_poisson, dict(workload="poisson", n=1000, precision="df64", steps=3,
+                                                          warmup=1, seed=0)),
+            ("batched_256_df64", bench_batched, dict(workload="batched", precision="df64", steps=1, warmup=1,
+                                                      seed=0)),
+            ("gnn_vs_jacobi_256_heldout", bench_gnn, dict(workload="gnn", precision="df64", steps=1, warmup=1,
+                                                          seed=1)))
+    for name, fn, over in runs:
+        a = copy.copy(args)
+        for k, v in over.items():
+            setattr(a, k, v)
+        a.no_cpu_baseline = True
+        t0 = time.perf_counter()
+        line = fn(a, world, rank, local)
+        keep = {k: line[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "dtype", "config", "solve",
+                                     "roofline", "e2e", "gpu_launches", "clocks") if k in line}
+        keep["wall_s"] = time.perf_counter() - t0
+        out[name] = keep
+        torch.cuda.empty_cache()
+    return out
 
 
 # ------------------------------------------------------------ reference --
@@ -656,77 +750,101 @@ def _bounded(step, steps, budget_s=REF_BUDGET_S):
     return done, time.perf_counter() - t0
 
 
-def bench_reference(args):
-    """The reference's CPU algorithm (oracle) on the host cores: each step one
-    full step / solve of the workload, as many of the requested steps as fit
-    REF_BUDGET_S (at most one warm-up step)."""
+def bench_reference(args, world):
+    """The reference's CPU algorithm (oracle: the aten ops its CPU backend
+    runs, in its order) on the host cores, with inputs built by the oracle's
+    own mesh, geometry and assembly restatements (nothing of this package's
+    native library runs here): each step one full step / solve of the
+    workload, as many of the requested steps as fit REF_BUDGET_S (at most
+    one warm-up step).  The config dict is the one our arm prints."""
+    from oracle import cg as ocg
+    from oracle import mesh as omesh
     torch.set_num_threads(os.cpu_count() or 1)
     requested = args.steps
     args.warmup = min(args.warmup, 1)
+    t_setup = time.perf_counter()
     if args.workload == "swe":
-        dtype = torch.float32 if args.dtype == "f32" else torch.float64
-        from easier_gb300 import mesh
         from oracle import swe as oswe
-        m = mesh.triangular_mesh(args.n)
-        g = mesh.swe_geometry(m)
-        p = oswe.SweProblem(m.src, m.dst, m.bcells, g.sx, g.sy, g.alpha, g.bsx, g.bsy, g.area, args.dt, dtype)
-        h = torch.from_numpy(mesh.gaussian_bump(g.x, g.y)).to(dtype)
+        dtype = torch.float32 if args.dtype == "f32" else torch.float64
+        m = omesh.triangular_mesh(args.n)
+        g = omesh.swe_geometry(m)
+        p = oswe.SweProblem(m["src"], m["dst"], m["bcells"], g["sx"], g["sy"], g["alpha"], g["bsx"], g["bsy"],
+                            g["area"], args.dt, dtype)
+        x, y = np.asarray(g["x"]), np.asarray(g["y"])
+        h = torch.from_numpy(1 + 0.1 * np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2) / 0.01)).to(dtype)
         st = [h, torch.zeros_like(h), torch.zeros_like(h)]
+        nc = int(h.shape[0])
 
         def one(_):
             st[:] = p.step(*st)
+        setup = time.perf_counter() - t_setup
         for _ in range(args.warmup):
             one(0)
         args.steps, wall = _bounded(one, requested)
-        v = m.nc * args.steps / wall
+        v = nc * args.steps / wall
         unit, metric = "cell-steps/s", "SWE cell-steps/s"
-        sample = f"{args.steps} full oracle steps at N={args.n} ({m.nc} cells), {args.dtype}"
-        cfg = {"workload": f"shallow water, tutorial mesh N={args.n} ({m.nc} cells, {m.ne} directed edges), dt={args.dt}"}
+        sample = f"{args.steps} full oracle steps at N={args.n} ({nc} cells), {args.dtype}"
+        cfg = swe_config(args, world)
     elif args.workload in ("batched", "gnn"):
-        from easier_gb300.numeric.batched import p1_instances
-        from oracle import cg as ocg
-        insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
-        order = np.random.default_rng(0).permutation(len(insts))
+        from easier_gb300 import mesh as gen  # numpy generators of the seeded fields and right hand sides
+        from easier_gb300.numeric.batched import p1_sides
+        sides = p1_sides(args.count, args.nmin, args.nmax, seed=args.seed)
+        order = np.random.default_rng(0).permutation(len(sides))
+        cache = {}
+
+        def instance(i):
+            if i not in cache:
+                n = int(sides[i])
+                kappa = gen.kappa_from_field(gen.gaussian_random_field(n, args.seed * 100_003 + 2 * i))
+                row, col, Ae, Av = omesh.p1_arrays(n, kappa)
+                b = gen.random_mode_rhs(n, args.seed * 100_003 + 2 * i + 1)
+                cache[i] = (row, col, Ae, Av, b, n)
+            return cache[i]
+        setup = time.perf_counter() - t_setup
         for i in order[:args.warmup]:
-            s = insts[i]
-            ocg.cg(s.row, s.col, s.Ae, s.Av, s.b, rtol=1e-8, jacobi=True)
+            row, col, Ae, Av, b, _ = instance(i)
+            ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)
         sizes = []
         timed = order[args.warmup:]
+        build_s = [0.0]
 
         def one(k):
-            s = insts[timed[k % len(timed)]]
-            ocg.cg(s.row, s.col, s.Ae, s.Av, s.b, rtol=1e-8, jacobi=True)
-            sizes.append(int(round(np.sqrt(s.n))) + 1)
+            t0 = time.perf_counter()
+            row, col, Ae, Av, b, n = instance(timed[k % len(timed)])
+            build_s[0] += time.perf_counter() - t0
+            ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)
+            sizes.append(n)
         args.steps, wall = _bounded(one, requested)
+        wall -= build_s[0]
         v = args.steps / wall
         unit, metric = "solves/s", "Poisson solves/s (batched)"
         sample = (f"{args.steps} full Jacobi-PCG solves of seeded instances drawn from the batch "
-                  f"(N={sizes}), one per step")
-        cfg = {"workload": f"batched P1 Poisson, {args.count} instances, N ~ U{{{args.nmin}..{args.nmax}}}, "
-                           f"Jacobi-PCG per instance to rel. residual 1e-8"}
+                  f"(N={sizes}), one per step (instance assembly not timed)")
+        cfg = batched_config(args, world)
     else:
-        from easier_gb300 import mesh
-        from oracle import cg as ocg
-        s = mesh.p1_system(args.n)
-        b = mesh.random_mode_rhs(args.n, 0)
+        from easier_gb300 import mesh as gen
+        row, col, Ae, Av = omesh.p1_arrays(args.n)
+        b = gen.random_mode_rhs(args.n, 0)
+        setup = time.perf_counter() - t_setup
         for _ in range(args.warmup):
-            ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-8, jacobi=True)
+            ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)
         its = []
 
         def one(_):
-            its.append(ocg.cg(s.row, s.col, s.Ae, s.Av, b, rtol=1e-8, jacobi=True)[1])
+            its.append(ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)[1])
         args.steps, wall = _bounded(one, requested)
-        it = its[-1]
         v = args.steps / wall
         unit, metric = "solves/s", "Poisson solves/s"
-        sample = f"{args.steps} full Jacobi-PCG solves ({it} iterations each) on the {args.n}x{args.n} P1 grid"
-        cfg = {"workload": f"P1 Poisson {args.n}x{args.n} grid, Jacobi-PCG to rel. residual 1e-8"}
+        sample = f"{args.steps} full Jacobi-PCG solves ({its[-1]} iterations each) on the {args.n}x{args.n} P1 grid"
+        cfg = poisson_config(args, world)
     cores = torch.get_num_threads()
     if args.steps < requested:
         sample += f"; {args.steps} of the {requested} requested steps fit the {REF_BUDGET_S:.0f} s budget"
-    return {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": 1, "steps": args.steps,
+    sample += f"; oracle input set-up {setup:.1f} s (not timed)"
+    return {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic", "config": cfg,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype if args.workload == "swe" else "f64",
+            "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -753,6 +871,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-solvers", action="store_true", help="swe: leave out the solver figures")
     ap.add_argument("--tile-cells", type=int, default=None, help="swe: target cells per tile (FP32 tiled step)")
     args = ap.parse_args()
     if args.n is None:
@@ -774,7 +893,7 @@ def main():
             args.warmup = {"swe": 1, "poisson": 0, "batched": 1, "gnn": 1}[args.workload]
         if rank != 0:
             return
-        print(json.dumps(bench_reference(args)), flush=True)
+        print(json.dumps(bench_reference(args, world)), flush=True)
         return
     if args.steps is None:
         args.steps = {"swe": 1000, "poisson": 10, "batched": 5, "gnn": 3}[args.workload]

@@ -411,8 +411,49 @@ static __device__ __align__(256) unsigned char g_agg_noalloc_scratch[ESR_AGG_NOA
 
 namespace {
 constexpr int kNoAllocMaxDevices = 64;
+// The array's device address belongs to one CUDA context: the primary
+// context of a device, recreated with a new address after cudaDeviceReset,
+// or a context the caller created with the driver API.  It is cached per
+// device together with the unique ID (cuCtxGetId) of the context it was
+// looked up in, and looked up again whenever the current context's ID
+// differs.
 std::mutex g_noalloc_mu;
-void *g_noalloc_addr[kNoAllocMaxDevices];  // device address of the array, per device
+struct NoAllocAddr {
+  unsigned long long ctx_id;
+  void *addr;
+};
+NoAllocAddr g_noalloc_addr[kNoAllocMaxDevices];
+
+using CtxGetCurrentFn = int (*)(void **);
+using CtxGetIdFn = int (*)(void *, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current;
+CtxGetIdFn g_ctx_get_id;
+
+// Driver entry points through the runtime (no link against libcuda).
+cudaError_t noalloc_driver_fns() {
+  if (g_ctx_get_current && g_ctx_get_id) return cudaSuccess;
+  void *a = nullptr, *b = nullptr;
+  cudaDriverEntryPointQueryResult qa, qb;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
+  if (e != cudaSuccess) return e;
+  e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+  if (e != cudaSuccess) return e;
+  if (qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+    return cudaErrorSymbolNotFound;
+  g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+  g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(b);
+  return cudaSuccess;
+}
+
+// ID of the context current on this thread; 0 when there is none yet.
+cudaError_t noalloc_ctx_id(unsigned long long *id) {
+  *id = 0;
+  void *ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0) return cudaErrorDeviceUninitialized;
+  if (!ctx) return cudaSuccess;
+  if (g_ctx_get_id(ctx, id) != 0) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
 }  // namespace
 
 extern "C" int esr_aggregate_noalloc(int dtype, int agg, const void *t, int64_t n, int64_t cols, void *out,
@@ -435,17 +476,28 @@ extern "C" int esr_aggregate_noalloc(int dtype, int agg, const void *t, int64_t 
   if (dev < 0 || dev >= kNoAllocMaxDevices) return esr::fail(ESR_ERR_UNSUPPORTED, "esr_aggregate_noalloc: device ordinal");
   void *ws = nullptr;
   {
-    // First call on this device: look up the array's device address (this
-    // is the set-up; it may load the module, so it must not be the first
-    // call inside a stream capture).
+    // Set-up, on the first call in a context: look up the array's device
+    // address (this may load the module, so it must not be the first call
+    // inside a stream capture).
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    e = noalloc_driver_fns();
+    if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/driver entry points");
+    unsigned long long id = 0;
+    e = noalloc_ctx_id(&id);
+    if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/current context");
+    NoAllocAddr &slot = g_noalloc_addr[dev];
+    if (id == 0 || slot.addr == nullptr || slot.ctx_id != id) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_agg_noalloc_scratch);
       if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/cudaGetSymbolAddress");
-      g_noalloc_addr[dev] = p;
+      if (id == 0) {  // the lookup made the device's primary context current
+        e = noalloc_ctx_id(&id);
+        if (e != cudaSuccess) return esr::cuda_check(e, "esr_aggregate_noalloc/current context");
+      }
+      slot.ctx_id = id;
+      slot.addr = p;
     }
-    ws = g_noalloc_addr[dev];
+    ws = slot.addr;
   }
   // Every partial slot the second launch reads is written by the first one,
   // so nothing needs clearing between calls.

@@ -484,21 +484,27 @@ class BatchedPCG:
 _TUNE_CACHE: dict = {}
 
 
+def p1_sides(count: int, nmin: int, nmax: int, seed: int = 0) -> np.ndarray:
+    """Mesh sides of a seeded batch: N ~ U{nmin..nmax}."""
+    return np.random.default_rng(seed).integers(nmin, nmax + 1, count)
+
+
+def p1_instance(i: int, n: int, seed: int = 0, corr_len: float = 0.1, variance: float = 1.0) -> LinsysInstance:
+    """Instance i of a seeded batch, of side n: kappa = exp(g) with g a
+    Gaussian random field (field seed 100003 * seed + 2i), 16-mode random
+    right hand side (seed 100003 * seed + 2i + 1)."""
+    kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, seed * 100_003 + 2 * i, corr_len, variance))
+    s = mesh.p1_system(n, kappa)
+    b = mesh.random_mode_rhs(n, seed * 100_003 + 2 * i + 1)
+    return LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, b, edge_len=p1_edge_length(n, s.row, s.col))
+
+
 def p1_instances(count: int, nmin: int, nmax: int, seed: int = 0, corr_len: float = 0.1,
                  variance: float = 1.0) -> List[LinsysInstance]:
     """Seeded batch of P1 Poisson instances: side N ~ U{nmin..nmax},
     kappa = exp(g) with g a Gaussian random field (correlation length
     corr_len, variance), 16-mode random right hand side."""
-    rng = np.random.default_rng(seed)
-    sides = rng.integers(nmin, nmax + 1, count)
-    out = []
-    for i, n in enumerate(sides):
-        n = int(n)
-        kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, seed * 100_003 + 2 * i, corr_len, variance))
-        s = mesh.p1_system(n, kappa)
-        b = mesh.random_mode_rhs(n, seed * 100_003 + 2 * i + 1)
-        out.append(LinsysInstance(s.nunk, s.row, s.col, s.Ae, s.Av, b, edge_len=p1_edge_length(n, s.row, s.col)))
-    return out
+    return [p1_instance(i, int(n), seed, corr_len, variance) for i, n in enumerate(p1_sides(count, nmin, nmax, seed))]
 
 
 def p1_edge_length(n: int, row: np.ndarray, col: np.ndarray) -> np.ndarray:

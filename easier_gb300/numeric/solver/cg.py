@@ -1,18 +1,19 @@
 """Conjugate gradient, easier/numeric/solver/cg.py.
 
-``Init``/``Step``/``Update`` are the reference's three modules (cg.py:12-71)
-and run on the per-op path for any operator ``A`` and preconditioner ``M``.
-``CG.solve`` uses the fused PCG kernels instead when ``A`` is a compiled
-``Linsys`` and ``M`` is None or ``Jacobi``: same iteration, same stopping
-test (cg.py:130-161), evaluated on the device.
+``CG.solve`` runs the fused PCG kernels when ``A`` is a compiled ``Linsys``
+and ``M`` is None or ``Jacobi``: the reference's iteration and stopping test
+(cg.py:130-161), evaluated on the device.  Any other operator or
+preconditioner runs ``pcg_per_op``: the same iteration as a loop over the
+package's device ops, calling ``A`` and ``M`` as given.
 """
 from __future__ import annotations
 
-from typing import Any, Dict, Optional
+from typing import Any, Callable, Dict, Optional
 
 import torch
 from torch import nn
 
+from ... import _lib
 from ... import module as esr
 from ... import ops
 from ...utils import logger
@@ -20,51 +21,84 @@ from ..linsys import Linsys
 from ..preconditioner.jacobi import Jacobi
 
 
-class Init(esr.Module):
-    def __init__(self, A, b, x, M, r, z, p, bnorm) -> None:
-        super().__init__()
-        self.A, self.x, self.b, self.M = A, x, b, M
-        self.r, self.z, self.p, self.bnorm = r, z, p, bnorm
-
-    def forward(self):
-        self.r[:] = self.b - self.A(self.x)
-        self.z[:] = self.M(self.r)
-        self.p[:] = self.z
-        self.bnorm[:] = esr.norm(self.b).norm()
-
-
-class Step(esr.Module):
-    def __init__(self, A, x, r, z, p, rnorm, rzsum):
-        super().__init__()
-        self.A, self.x, self.p, self.r, self.z = A, x, p, r, z
-        self.rnorm, self.rzsum = rnorm, rzsum
-
-    def forward(self):
-        Ap = self.A(self.p)
-        rzsum = esr.sum(self.r * self.z).sum()
-        alpha = rzsum / esr.sum(self.p * Ap).sum()
-        r1 = self.r - alpha * Ap
-        self.x.add_(alpha * self.p)
-        self.rzsum[:] = rzsum
-        self.r[:] = r1
-        self.rnorm[:] = esr.norm(r1).norm()
-
-
-class Update(esr.Module):
-    def __init__(self, x, M, r, z, p, rzsum):
-        super().__init__()
-        self.x, self.M, self.r, self.z, self.p, self.rzsum = x, M, r, z, p, rzsum
-
-    def forward(self):
-        z1 = self.M(self.r)
-        beta = esr.sum(self.r * z1).sum() / self.rzsum
-        p1 = z1 + beta * self.p
-        self.z[:] = z1
-        self.p[:] = p1
-
-
 def _identity(x):
     return x
+
+
+class _Dots:
+    """FP64-accumulated dot products of one vector length (esr_dot), sharing
+    one zeroed workspace (the kernel's arrival counter resets itself)."""
+
+    def __init__(self, like: torch.Tensor) -> None:
+        nbytes = int(_lib.lib().esr_dot_workspace_bytes(like.numel()))
+        self.ws = torch.zeros(max(nbytes, 16), dtype=torch.uint8, device=like.device)
+
+    def __call__(self, u: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+        return ops.dot(u.reshape(-1), v.reshape(-1), workspace=self.ws)
+
+
+def pcg_per_op(A: Callable, M: Callable, b: torch.Tensor, x: torch.Tensor, r: torch.Tensor, z: torch.Tensor,
+               p: torch.Tensor, rtol: float, atol: Optional[float], maxiter: Optional[int],
+               on_iter: Callable[[int, float], None] = lambda it, rn: None):
+    """Preconditioned CG for any operator ``A`` and preconditioner ``M``
+    (callables on device tensors of x's shape), one device op at a time.
+
+    Iteration and stopping test as the reference's (cg.py:74-137): after
+    each update of x and r, stop when the recurrence residual norm is at
+    most max(rtol * ||b||, atol) (a NaN norm never stops it) or the update
+    count has reached ``maxiter``; otherwise precondition and form the next
+    direction p = z + (r.z / r_old.z_old) p.  r.z is kept from one
+    iteration to the next.  Dots accumulate in FP64; the scalars reach the
+    vector updates in x's dtype.  ``x`` is updated in place and ``r``, ``z``,
+    ``p`` hold the last residual, preconditioned residual and direction.
+    Returns (residual norm, r.z, ||b||, update count)."""
+    dot = _Dots(x)
+    bnorm = float(dot(b, b).sqrt())
+    tol = rtol * bnorm
+    if atol:
+        tol = max(tol, atol)
+    r.copy_(b - A(x))
+    z.copy_(M(r))
+    p.copy_(z)
+    rz = dot(r, z)
+    it = 0
+    while True:
+        q = A(p)
+        alpha = (rz / dot(p, q)).to(x.dtype)
+        x.add_(alpha * p)
+        r.sub_(alpha * q)
+        rnorm = float(dot(r, r).sqrt())
+        on_iter(it, rnorm)
+        if (rnorm == rnorm and rnorm <= tol) or (maxiter is not None and it >= maxiter):
+            return rnorm, float(rz), bnorm, it
+        it += 1
+        z.copy_(M(r))
+        rz_next = dot(r, z)
+        p.mul_((rz_next / rz).to(p.dtype)).add_(z)
+        rz = rz_next
+
+
+class _PlanCache:
+    """The fused plan of a Linsys, kept while the operator's values are the
+    ones it was built from.  The values are compared, not version counters:
+    writes through ``tensor.data`` (the usual way to refill an esr.Tensor)
+    leave the counters unchanged."""
+
+    def __init__(self) -> None:
+        self.plan = None
+        self.key = None
+        self.values = None
+
+    def get(self, key, A, build):
+        Ae, Av = A.Ae.data, A.Av.data
+        same = (self.plan is not None and self.key == key and self.values is not None
+                and self.values[0].shape == Ae.shape and self.values[1].shape == Av.shape
+                and torch.equal(self.values[0], Ae) and torch.equal(self.values[1], Av))
+        if not same:
+            self.plan = build()
+            self.key = key
+            self.values = (Ae.clone(), Av.clone())
+        return self.plan
 
 
 class CG(esr.Module):
@@ -82,11 +116,8 @@ class CG(esr.Module):
         self.rzsum = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
         self.rnorm = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
         self.bnorm = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
-        self.init = Init(A, b, x, self.M, self.r, self.z, self.p, self.bnorm)
-        self.step = Step(A, x, self.r, self.z, self.p, self.rnorm, self.rzsum)
-        self.update = Update(x, self.M, self.r, self.z, self.p, self.rzsum)
+        self._plans = _PlanCache()
         self._fused = None
-        self._fused_key = None
         self.last_info: Dict[str, Any] = {}
 
     # ------------------------------------------------------------ fused --
@@ -109,24 +140,25 @@ class CG(esr.Module):
         'mixed' on MixedPCG."""
         from ..sparse import FusedPCG, MixedPCG, SellMatrix
         A = self.A
-        key = (precision, A.Ae.data.data_ptr(), A.Ae._version, A.Av.data.data_ptr(), A.Av._version)
-        if self._fused is None or self._fused_key != key:
+
+        def build():
             jacobi = isinstance(self.M, Jacobi)
             if precision in ("mixed", "df64") and A.Av.dtype != torch.float64:
                 raise ValueError(f"precision='{precision}' needs an FP64 system")
             if precision == "mixed":
-                self._fused = MixedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
-            elif precision == "df64" or A.Av.dtype == torch.float64:
+                return MixedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
+            if precision == "df64" or A.Av.dtype == torch.float64:
                 from ..batched import BatchedPCG, LinsysInstance
                 n = A.Av.shape[0]
                 inst = LinsysInstance(n, A.reducer.idx.detach().cpu().numpy(), A.selector.idx.detach().cpu().numpy(),
                                       A.Ae.data, A.Av.data, self.b.data)
-                self._fused = BatchedPCG([inst], jacobi=jacobi, precision="df64" if precision == "df64" else "fp64",
-                                         device=self.x.device)
-                self._fused.autotune()
-            else:
-                self._fused = FusedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
-            self._fused_key = key
+                eng = BatchedPCG([inst], jacobi=jacobi, precision="df64" if precision == "df64" else "fp64",
+                                 device=self.x.device)
+                eng.autotune()
+                return eng
+            return FusedPCG(SellMatrix.from_linsys(A), jacobi=jacobi)
+
+        self._fused = self._plans.get((precision, isinstance(self.M, Jacobi)), A, build)
         return self._fused
 
     def solve(self, rtol: float = 1e-5, atol: Optional[float] = None, maxiter: Optional[int] = None,
@@ -150,21 +182,17 @@ class CG(esr.Module):
             return self._solve_fused(rtol, atol, maxiter, precision)
         if precision != "native":
             raise ValueError(f"precision='{precision}' needs the fused path (Linsys operator, Jacobi or no preconditioner)")
-        self.init()
-        rtol_t = rtol * self.bnorm
-        tol = torch.maximum(rtol_t, torch.as_tensor(atol, dtype=rtol_t.dtype, device=rtol_t.device)) \
-            if atol else rtol_t
-        iters = 0
-        while True:
-            self.step()
-            if debug_iter is not None and iters % debug_iter == 0:
-                logger.info(f"{name} residual {float(self.rnorm)} at the {iters}-th iteration")
-            if (not torch.isnan(self.rnorm) and self.rnorm <= tol) or (maxiter is not None and iters >= maxiter):
-                break
-            iters += 1
-            self.update()
-        logger.info(f"{name} solver completed with residual {float(self.rnorm)} at the {iters}-th iteration")
-        self.last_info = {"residual": float(self.rnorm), "iters": iters}
+
+        def log(it, rn):
+            if debug_iter is not None and it % debug_iter == 0:
+                logger.info(f"{name} residual {rn} at the {it}-th iteration")
+        rnorm, rz, bnorm, iters = pcg_per_op(self.A, self.M, self.b.data, self.x.data, self.r.data, self.z.data,
+                                             self.p.data, rtol, atol, maxiter, log)
+        self.rnorm.data.fill_(rnorm)
+        self.rzsum.data.fill_(rz)
+        self.bnorm.data.fill_(bnorm)
+        logger.info(f"{name} solver completed with residual {rnorm} at the {iters}-th iteration")
+        self.last_info = {"residual": rnorm, "iters": iters}
         return dict(self.last_info)
 
     def _solve_fused(self, rtol, atol, maxiter, precision) -> Dict[str, Any]:

@@ -1,112 +1,125 @@
 """Restarted GMRES, easier/numeric/solver/gmres.py.
 
-The Arnoldi process keeps the reference's structure (modified Gram-Schmidt
-through small modules, Hessenberg least squares by SVD on the host,
-gmres.py:12-266); every Linsys application, dot product and norm inside it
-runs in the GB300 kernels.
+``GMRES.solve`` runs every restart cycle as one CUDA graph of fused kernels
+(``sparse.FusedGMRES``) when ``A`` is a compiled ``Linsys`` and ``M`` is None
+or ``Jacobi``.  Any other operator or preconditioner runs
+``gmres_per_op``: restarted, right-preconditioned GMRES as a loop over the
+package's device ops, calling ``A`` and ``M`` as given.  Both stop on the
+reference's test (gmres.py:222-266): the true residual norm at the start of
+a cycle against max(rtol * ||b||, atol), counting cycles.
 """
 from __future__ import annotations
 
-from typing import Any, Dict, Optional
+import math
+from typing import Any, Callable, Dict, Optional
 
+import numpy as np
 import torch
 from torch import nn
 
 from ... import module as esr
 from ...utils import logger
+from .cg import _Dots, _PlanCache
 
-
-class UpdateRnorm(esr.Module):
-    def __init__(self, A, b, x, r, rnorm):
-        super().__init__()
-        self.A, self.b, self.x, self.r, self.rnorm = A, b, x, r, rnorm
-
-    def forward(self):
-        r = self.b - self.A(self.x)
-        self.r[:] = r
-        self.rnorm[:] = esr.norm(r).norm()
-
-
-class Init(esr.Module):
-    def __init__(self, b, bnorm) -> None:
-        super().__init__()
-        self.b, self.bnorm = b, bnorm
-
-    def forward(self) -> None:
-        self.bnorm[:] = esr.norm(self.b).norm()
-
-
-class InitV(esr.Module):
-    def __init__(self, r, rnorm, V):
-        super().__init__()
-        self.r, self.rnorm, self.V = r, rnorm, V
-
-    def forward(self):
-        self.V[:, ..., 0] = self.r / self.rnorm
-
-
-class InitW(esr.Module):
-    def __init__(self, A, M, V, w):
-        super().__init__()
-        self.A, self.M, self.V, self.w = A, M, V, w
-        self.j = esr.Tensor(torch.tensor([0], dtype=torch.int32, device=V.device), mode="replicate")
-
-    def forward(self):
-        self.w[:] = self.A(self.M(self.V[:, ..., self.j].squeeze(-1)))
-
-
-class SumW(esr.Module):
-    def __init__(self, V, w, h):
-        super().__init__()
-        self.V, self.w, self.h = V, w, h
-        self.i = esr.Tensor(torch.tensor([0], dtype=torch.int32, device=V.device), mode="replicate")
-
-    def forward(self):
-        self.h[:] = esr.sum(self.V[:, ..., self.i].squeeze(-1) * self.w).sum()
-
-
-class NormW(esr.Module):
-    def __init__(self, w, h):
-        super().__init__()
-        self.w, self.h = w, h
-
-    def forward(self):
-        self.h[:] = esr.norm(self.w).norm()
-
-
-class UpdateW(esr.Module):
-    def __init__(self, V, w, h):
-        super().__init__()
-        self.V, self.w, self.h = V, w, h
-        self.i = esr.Tensor(torch.tensor([0], dtype=torch.int32, device=V.device), mode="replicate")
-
-    def forward(self):
-        self.w.sub_(self.h * self.V[:, ..., self.i].squeeze(-1))
-
-
-class UpdateV(esr.Module):
-    def __init__(self, V, w, h):
-        super().__init__()
-        self.V, self.w, self.h = V, w, h
-        self.i = esr.Tensor(torch.tensor([0], dtype=torch.int32, device=V.device), mode="replicate")
-
-    def forward(self):
-        self.V[:, ..., self.i] = (self.w / self.h)[:, ..., None]
-
-
-class UpdateX(esr.Module):
-    def __init__(self, x, V, M, y, i):
-        super().__init__()
-        self.x, self.V, self.M, self.y, self.i = x, V, M, y, i
-
-    def forward(self):
-        V = self.V[:, ..., :self.i]
-        dx = torch.matmul(V, self.y[:self.i]).squeeze(dim=-1)
-        self.x.add_(self.M(dx))
+# an Arnoldi step whose new basis norm falls below this has found an
+# invariant subspace: the cycle ends there (the reference's threshold)
+BREAKDOWN = 1e-15
 
 
 def _identity(x):
     return x
+
+
+class _GivensLS:
+    """min_y || beta e1 - H y || for the (j+2) x (j+1) Hessenberg matrices of
+    one Arnoldi cycle, reduced to an upper triangle by one Givens rotation
+    per column as the columns arrive (FP64, host)."""
+
+    def __init__(self, m: int, beta: float) -> None:
+        self.R = np.zeros((m + 1, m))
+        self.g = np.zeros(m + 1)
+        self.g[0] = beta
+        self.cs = np.zeros(m)
+        self.sn = np.zeros(m)
+        self.k = 0
+
+    def add_column(self, h: np.ndarray) -> None:
+        """h: column j of H, entries 0..j+1."""
+        j = self.k
+        h = np.array(h, dtype=np.float64)
+        for i in range(j):  # earlier rotations
+            a, b = h[i], h[i + 1]
+            h[i] = self.cs[i] * a + self.sn[i] * b
+            h[i + 1] = -self.sn[i] * a + self.cs[i] * b
+        a, b = h[j], h[j + 1]
+        rho = math.hypot(a, b)
+        c, s = (1.0, 0.0) if rho == 0.0 else (a / rho, b / rho)
+        self.cs[j], self.sn[j] = c, s
+        h[j], h[j + 1] = rho, 0.0
+        self.R[: j + 2, j] = h[: j + 2]
+        self.g[j + 1] = -s * self.g[j]
+        self.g[j] = c * self.g[j]
+        self.k = j + 1
+
+    def solve(self) -> np.ndarray:
+        """y of the columns added so far (back substitution; a zero pivot,
+        which only an exactly singular H gives, contributes zero)."""
+        k = self.k
+        y = np.zeros(k)
+        for i in range(k - 1, -1, -1):
+            t = self.g[i] - self.R[i, i + 1:k] @ y[i + 1:]
+            y[i] = t / self.R[i, i] if self.R[i, i] != 0.0 else 0.0
+        return y
+
+
+def gmres_per_op(A: Callable, M: Callable, b: torch.Tensor, x: torch.Tensor, r: torch.Tensor, restart: int,
+                 rtol: float, atol: Optional[float], maxiter: Optional[int],
+                 on_cycle: Callable[[int, float], None] = lambda it, rn: None):
+    """Restarted GMRES(restart) with right preconditioner ``M`` for any
+    operator ``A`` (callables on device tensors of x's shape).
+
+    Each cycle: r = b - A x and its norm (the stopping test: at most
+    max(rtol * ||b||, atol), NaN never stops, or ``maxiter`` cycles done);
+    then an orthonormal basis of the Krylov space of A M from r by modified
+    Gram-Schmidt (FP64 dot products, basis rows contiguous in device
+    memory), the least-squares problem reduced by Givens rotations on the
+    host as each Hessenberg column arrives, and x += M(V^T y).  ``x`` is
+    updated in place, ``r`` holds the last residual.
+    Returns (residual norm, ||b||, cycles)."""
+    dot = _Dots(x)
+    n = x.numel()
+    bnorm = float(dot(b, b).sqrt())
+    tol = rtol * bnorm
+    if atol:
+        tol = max(tol, atol)
+    V = torch.empty((restart + 1, n), dtype=x.dtype, device=x.device)
+    hcol = torch.empty(restart + 1, dtype=torch.float64, device=x.device)
+    cycles = 0
+    while True:
+        r.copy_(b - A(x))
+        beta = float(dot(r, r).sqrt())
+        on_cycle(cycles, beta)
+        if (beta == beta and beta <= tol) or (maxiter is not None and cycles >= maxiter):
+            return beta, bnorm, cycles
+        cycles += 1
+        ls = _GivensLS(restart, beta)
+        V[0].copy_(r.reshape(-1) / beta)
+        for j in range(restart):
+            w = A(M(V[j].view(x.shape))).reshape(-1).clone()
+            for i in range(j + 1):
+                hij = dot(V[i], w)
+                hcol[i:i + 1].copy_(hij)
+                w.sub_(hij.to(w.dtype) * V[i])
+            hcol[j + 1:j + 2].copy_(dot(w, w).sqrt())
+            col = hcol[: j + 2].cpu().numpy()
+            ls.add_column(col)
+            if col[j + 1] < BREAKDOWN:
+                break
+            if j + 1 < restart:
+                V[j + 1].copy_(w / col[j + 1])
+        y = torch.from_numpy(ls.solve()).to(device=x.device, dtype=x.dtype)
+        dx = (y.unsqueeze(0) @ V[: ls.k]).view(x.shape)
+        x.add_(M(dx))
 
 
 class GMRES(esr.Module):
@@ -119,22 +132,9 @@ class GMRES(esr.Module):
         self.restart = restart
         self.r = esr.Tensor(esr.zeros_like(x), mode="partition")
         self.rnorm = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
-        self.update_rnorm = UpdateRnorm(A, b, x, self.r, self.rnorm)
         self.bnorm = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
-        self.init = Init(self.b, self.bnorm)
-        self.H = esr.Tensor(torch.zeros((restart + 1, restart), device=x.device, dtype=x.dtype), mode="replicate")
-        self.B = esr.Tensor(torch.zeros((restart + 1, 1), device=x.device, dtype=x.dtype), mode="replicate")
-        self.V = esr.Tensor(esr.zeros(tuple(x.shape) + (restart,), dtype=x.dtype, device=x.device), mode="partition")
-        self.init_V = InitV(self.r, self.rnorm, self.V)
-        self.w = esr.Tensor(esr.zeros_like(x), mode="partition")
-        self.init_w = InitW(A, self.M, self.V, self.w)
-        self.h = esr.Tensor(torch.tensor([0.0], dtype=x.dtype, device=x.device), mode="replicate")
-        self.sum_w = SumW(self.V, self.w, self.h)
-        self.update_w = UpdateW(self.V, self.w, self.h)
-        self.norm_w = NormW(self.w, self.h)
-        self.update_V = UpdateV(self.V, self.w, self.h)
-        self.y = esr.Tensor(torch.zeros((restart, 1), dtype=x.dtype, device=x.device), mode="replicate")
-        self.update_x = nn.ModuleList([UpdateX(self.x, self.V, self.M, self.y, i) for i in range(1, restart + 1)])
+        self._plans = _PlanCache()
+        self._fused = None
 
     # ------------------------------------------------------------ fused --
     def fusable(self) -> bool:
@@ -152,65 +152,32 @@ class GMRES(esr.Module):
     def _fused_solver(self):
         from ..preconditioner.jacobi import Jacobi
         from ..sparse import FusedGMRES, SellMatrix
-        A = self.A
-        key = (A.Ae.data.data_ptr(), A.Ae._version, A.Av.data.data_ptr(), A.Av._version, self.restart)
-        if getattr(self, "_fused", None) is None or self._fused_key != key:
-            self._fused = FusedGMRES(SellMatrix.from_linsys(A), self.restart, jacobi=isinstance(self.M, Jacobi))
-            self._fused_key = key
+        jacobi = isinstance(self.M, Jacobi)
+        self._fused = self._plans.get(
+            (self.restart, jacobi), self.A,
+            lambda: FusedGMRES(SellMatrix.from_linsys(self.A), self.restart, jacobi=jacobi))
         return self._fused
 
     def solve(self, rtol: float = 1e-5, atol: Optional[float] = None, maxiter: Optional[int] = None,
               debug_iter: Optional[int] = None, *, fused: Optional[bool] = None) -> Dict[str, Any]:
-        """Solve to ``rnorm <= max(rtol*||b||, atol)`` (gmres.py:222-266).
-        With a compiled ``Linsys`` and ``M`` None or ``Jacobi`` every restart
-        cycle runs as one CUDA graph of fused kernels (``fused=False``
-        forces the per-op modules)."""
+        """Solve to ``rnorm <= max(rtol*||b||, atol)`` (gmres.py:222-266),
+        counting restart cycles.  With a compiled ``Linsys`` and ``M`` None
+        or ``Jacobi`` every restart cycle runs as one CUDA graph of fused
+        kernels (``fused=False`` forces ``gmres_per_op``)."""
         name = self.__class__.__name__
+
+        def log(it, rn):
+            if debug_iter is not None and it % debug_iter == 0:
+                logger.info(f"{name} residual {rn} at the {it}-th iteration")
         use_fused = self.fusable() if fused is None else fused
         if use_fused:
             eng = self._fused_solver()
-
-            def log(it, rn):
-                if debug_iter is not None and it % debug_iter == 0:
-                    logger.info(f"{name} residual {rn} at the {it}-th iteration")
             s, iters = eng.solve(self.b.data, self.x.data, self.r.data, rtol, atol, maxiter, log)
-            self.rnorm.data.fill_(s.rnorm)
-            self.bnorm.data.fill_(s.bnorm)
-            logger.info(f"{name} solver completed with residual {s.rnorm} at the {iters}-th iteration")
-            return {"residual": float(s.rnorm), "iters": iters}
-        self.init()
-        rtol_t = rtol * self.bnorm
-        tol = torch.maximum(rtol_t, torch.as_tensor(atol, dtype=rtol_t.dtype, device=rtol_t.device)) \
-            if atol else rtol_t
-        iters = 0
-        while True:
-            self.update_rnorm()
-            if debug_iter is not None and iters % debug_iter == 0:
-                logger.info(f"{name} residual {float(self.rnorm)} at the {iters}-th iteration")
-            if (not torch.isnan(self.rnorm) and self.rnorm <= tol) or (maxiter is not None and iters >= maxiter):
-                break
-            iters += 1
-            self.B[0, 0] = self.rnorm
-            self.init_V()
-            for j in range(self.restart):
-                self.init_w.j.fill_(j)
-                self.init_w()
-                for i in range(j + 1):
-                    self.sum_w.i.fill_(i)
-                    self.sum_w()
-                    self.H[i, j] = self.h
-                    self.update_w.i.fill_(i)
-                    self.update_w()
-                self.norm_w()
-                self.H[j + 1, j] = self.h
-                if self.h < 1e-15:
-                    break
-                elif j < self.restart - 1:
-                    self.update_V.i.fill_(j + 1)
-                    self.update_V()
-            u, s, vt = torch.linalg.svd(self.H[:j + 2], full_matrices=False)
-            self.y[:] = vt.transpose(0, 1) @ torch.diag_embed(1 / torch.clamp(s, min=1e-8)) @ \
-                u.transpose(0, 1) @ self.B[:j + 2]
-            self.update_x[j]()
-        logger.info(f"{name} solver completed with residual {float(self.rnorm)} at the {iters}-th iteration")
-        return {"residual": float(self.rnorm), "iters": iters}
+            rnorm, bnorm = float(s.rnorm), float(s.bnorm)
+        else:
+            rnorm, bnorm, iters = gmres_per_op(self.A, self.M, self.b.data, self.x.data, self.r.data,
+                                               self.restart, rtol, atol, maxiter, log)
+        self.rnorm.data.fill_(rnorm)
+        self.bnorm.data.fill_(bnorm)
+        logger.info(f"{name} solver completed with residual {rnorm} at the {iters}-th iteration")
+        return {"residual": rnorm, "iters": iters}

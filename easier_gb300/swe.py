@@ -321,14 +321,14 @@ class SweEngine:
         return s
 
     def touched_bytes_per_step(self) -> int:
-        """HBM bytes one step must move in this layout (each array once)."""
+        """HBM bytes one step must move in this layout, each array once."""
         s = 8 if self.dtype == torch.float64 else 4
         nc, w = self.nc, self.width
         if self.tiled:
             st = self.tile_stats
             l3 = st["l3_over_own"] * nc
             loc = st["local_over_own"] * nc
-            geom = l3 * (3 * (4 + 3 * s) + s)
+            geom = l3 * (48 + (4 if self.precision == "exact" else 0))
             halo_idx = (loc - nc) * 4
             return int(geom + halo_idx + loc * 16 + nc * 16 + self.ntiles * 48)
         geom = nc * (w * (4 + 3 * s) + s)
@@ -337,6 +337,20 @@ class SweEngine:
         k2 = geom + 3 * st + 2 * st
         k4 = geom + 3 * st + st
         return k1 + 2 * k2 + k4
+
+    def bytes_model(self) -> str:
+        """The byte count touched_bytes_per_step() makes, in words."""
+        if self.tiled:
+            return ("per step: three 16-byte face records of every cell of halo level <= 3 (sx, sy, alpha, local "
+                    "neighbour" + ("; plus its area" if self.precision == "exact" else "; sx, sy pre-divided by the "
+                    "area") + "), the 16-byte state of every cell of level <= 4 and the 4-byte global index of "
+                    "each halo cell, the 16-byte new state of every cell, 48 bytes of tile metadata")
+        return ("per stage launch: face slots (neighbour index, sx, sy, alpha) and area of every cell, the stage "
+                "state in, the base state and the delta sum in and out, the stage state out")
+
+    def traffic_key(self) -> str:
+        """Key of this kernel variant's measured DRAM bytes per launch."""
+        return f"swe_tiled_{self.precision}"
 
 
 def slot_width(nc: int, nd: np.ndarray, nb: np.ndarray) -> int:

@@ -191,8 +191,11 @@ int esr_aggregate(int dtype, int agg, const void *t, int64_t n, int64_t cols,
  * device, kept until the process exits; sizes needing more
  * (esr_aggregate_workspace_bytes(n, cols) > ESR_AGG_NOALLOC_SCRATCH_BYTES;
  * every cols <= ESR_AGG_NOALLOC_MAX_COLS fits) are rejected with
- * ESR_ERR_ARG.  The first call on a device looks up the array's address
- * (make that call before any stream capture).  All calls share the array:
+ * ESR_ERR_ARG.  The first call in a CUDA context looks up the array's
+ * address in that context (make that call before any stream capture); the
+ * address is kept with the context's unique ID, so a call after
+ * cudaDeviceReset, or under another context of the same device, looks it
+ * up again instead of using a stale one.  All calls share the array:
  * calls that overlap on the GPU (different streams, no ordering) race. */
 #define ESR_AGG_NOALLOC_SCRATCH_BYTES (1 << 20)
 #define ESR_AGG_NOALLOC_MAX_COLS 64

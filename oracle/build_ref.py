@@ -7,16 +7,32 @@ installed).  The result is test infrastructure: ``tests/golden/make_golden.py``
 uses it (as ``easier.cpp_extension``) to run the reference here.  Nothing
 here is imported by the product.  Outputs only into ``oracle/_ref/``
 (git-ignored).  Usage: ``python oracle/build_ref.py [REFERENCE_ROOT]``.
+
+The reference tree is found by ``reference_root()``: ``EASIER_REFERENCE_ROOT``
+when set, else the read-only mount this recipe was written against, else
+nothing (and every caller skips the reference build).  This recipe is the
+only file that names that mount.
 """
 import os
 import sys
 from pathlib import Path
 
 OUT = Path(__file__).resolve().parent / "_ref"
-DEFAULT_REF = Path(os.environ.get("EASIER_REFERENCE_ROOT", "/root/reference"))
+_MOUNT = Path("/root/reference")
 
 
-def build(ref_root: Path = DEFAULT_REF, verbose: bool = False):
+def reference_root():
+    """The EASIER source tree to build from, or None when there is none."""
+    env = os.environ.get("EASIER_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    return _MOUNT if (_MOUNT / "csrc").is_dir() else None
+
+
+def build(ref_root=None, verbose: bool = False):
+    ref_root = ref_root if ref_root is not None else reference_root()
+    if ref_root is None:
+        raise FileNotFoundError("no reference tree: set EASIER_REFERENCE_ROOT")
     from torch.utils.cpp_extension import load
     ref_root = Path(ref_root)
     srcs = [ref_root / "csrc" / f for f in ("init.cpp", "triangular_mesh.cpp", "distpart.cpp")]
@@ -29,5 +45,5 @@ def build(ref_root: Path = DEFAULT_REF, verbose: bool = False):
 
 
 if __name__ == "__main__":
-    mod = build(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF, verbose=True)
+    mod = build(Path(sys.argv[1]) if len(sys.argv) > 1 else None, verbose=True)
     print(mod.__file__)

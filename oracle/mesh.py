@@ -191,3 +191,14 @@ def p1_system(n: int, kappa=None):
                         A[(ia, ib)] = A.get((ia, ib), 0.0) + v
     Av = np.array([A[(u, u)] for u in range(nunk)])
     return Av, A
+
+
+def p1_arrays(n: int, kappa=None):
+    """``p1_system`` as Linsys arrays: (row, col, Ae, Av) with the
+    off-diagonal couplings sorted by row, then column."""
+    Av, A = p1_system(n, kappa)
+    keys = sorted(k for k in A if k[0] != k[1])
+    row = np.array([k[0] for k in keys], dtype=np.int64)
+    col = np.array([k[1] for k in keys], dtype=np.int64)
+    Ae = np.array([A[k] for k in keys], dtype=np.float64)
+    return row, col, Ae, Av

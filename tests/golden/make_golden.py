@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory by running the reference.
 
-Runs the EASIER reference package itself (imported from its source tree,
-default ``/root/reference``, override with ``EASIER_REFERENCE_ROOT``) on its
+Runs the EASIER reference package itself (imported from its source tree:
+``EASIER_REFERENCE_ROOT``, else the tree ``oracle/build_ref.py`` finds) on its
 CPU backend at world size 1, with its C++ extension compiled by
 ``oracle/build_ref.py``.  ``h5py`` / ``more_itertools`` / ``matplotlib`` are
 absent here, so ``_stubs/`` stands in for them and the tutorial's HDF5 files
@@ -30,7 +30,6 @@ os.environ.setdefault("EASIER_LOG_LEVEL", "WARNING")
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF = Path(os.environ.get("EASIER_REFERENCE_ROOT", "/root/reference"))
 
 import numpy as np  # noqa: E402
 import torch  # noqa: E402
@@ -40,6 +39,9 @@ sys.path.insert(0, str(HERE / "_stubs"))
 sys.path.insert(0, str(ROOT / "oracle"))
 import build_ref  # noqa: E402
 
+REF = build_ref.reference_root()
+if REF is None:
+    sys.exit("make_golden: no reference tree (set EASIER_REFERENCE_ROOT)")
 _ext = build_ref.build(REF)
 sys.modules["easier.cpp_extension"] = _ext
 sys.path.insert(0, str(REF))

@@ -192,3 +192,52 @@ def test_fp32_system_uses_single_system_kernels():
     assert np.linalg.norm(x - x_ref.numpy()) <= 1e-3 * np.linalg.norm(x_ref.numpy())
     tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, b, x)
     assert tr <= 2e-5 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("solver", ["cg", "gmres"])
+def test_fused_plan_follows_operator_values_changed_through_data(solver):
+    """Refilling Ae/Av through ``.data`` (which leaves version counters
+    alone) between two solves must rebuild the fused plan: scaling the
+    operator by 2 halves the solution."""
+    eqn = workloads.P1Poisson(16, rhs_seed=0)
+    M = Jacobi(eqn.A)
+    sol = CG(eqn.A, eqn.b, eqn.x, M=M) if solver == "cg" else GMRES(eqn.A, eqn.b, eqn.x, M=M, restart=10)
+    [eqn, sol] = esr.compile([eqn, sol], "cuda")
+    sol.solve(rtol=1e-11, maxiter=500)
+    x1 = eqn.x.collect().clone()
+    plan = sol._fused
+    eqn.A.Ae.data.mul_(2)
+    eqn.A.Av.data.mul_(2)
+    eqn.x.data.zero_()
+    sol.solve(rtol=1e-11, maxiter=500)
+    assert sol._fused is not plan
+    assert torch.allclose(eqn.x.collect(), x1 / 2, rtol=1e-8, atol=1e-14)
+    # unchanged values keep the plan
+    plan = sol._fused
+    eqn.x.data.zero_()
+    sol.solve(rtol=1e-11, maxiter=500)
+    assert sol._fused is plan
+
+
+def test_per_op_paths_take_any_operator_and_preconditioner():
+    """A plain nn.Module operator (not a Linsys) and a callable
+    preconditioner run the per-op CG and GMRES loops; both reach the
+    tolerance on the FP64 true residual of the same system."""
+    from torch import nn
+    eqn = workloads.P1Poisson(20, rhs_seed=2)
+    [eqn] = esr.compile([eqn], "cuda")
+    A = eqn.A
+
+    class Op(nn.Module):
+        def forward(self, v):
+            return A(v)
+    s = mesh.p1_system(20)
+    b = eqn.b.collect().cpu().numpy()
+    for make in (lambda: CG(Op(), eqn.b, eqn.x, M=lambda r: r / A.Av),
+                 lambda: GMRES(Op(), eqn.b, eqn.x, M=lambda r: r / A.Av, restart=15)):
+        sol = make()
+        assert not sol.fusable()
+        eqn.x.data.zero_()
+        info = sol.solve(rtol=1e-9, maxiter=3000)
+        tr = ocg.true_residual(s.row, s.col, s.Ae, s.Av, b, eqn.x.collect().cpu().numpy())
+        assert tr <= 1.05e-9 * np.linalg.norm(b), (type(sol).__name__, info, tr)
