@@ -38,6 +38,9 @@ class SweTiles(Structure):
                 ("pad2_", c_int32)]
 
 
+SWE_TILE_AUTO, SWE_TILE_BLOCKED, SWE_TILE_PIPELINED = 0, 1, 2
+
+
 class Sell(Structure):
     _fields_ = [("n", c_int64), ("nslots", c_int64), ("dtype", c_int32), ("pad_", c_int32),
                 ("slice_ptr", c_void_p), ("col", c_void_p), ("val", c_void_p), ("diag", c_void_p)]
@@ -108,6 +111,8 @@ _SIGS = {
     "esr_swe_tile_smem_bytes": (c_int64, [POINTER(SweTiles)]),
     "esr_swe_tile_threads": (c_int, [POINTER(SweTiles)]),
     "esr_swe_tile_step": (c_int, [POINTER(SweTiles), c_double, _P, _P, c_int64, _P]),
+    "esr_swe_tile_kernel": (c_int, [POINTER(SweTiles)]),
+    "esr_swe_tile_step_with": (c_int, [POINTER(SweTiles), c_int, c_double, _P, _P, c_int64, _P]),
     "esr_bisect_partition": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P]),
     "esr_swe_tile_layout": (c_int, [c_int64, _P, _P, c_int64, _P, POINTER(c_int64), POINTER(c_int64), _P, _P, _P,
                                     _P, _P, _P]),
@@ -141,7 +146,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 9
+ABI_VERSION = 10
 
 
 def library_path() -> Path:

@@ -609,6 +609,376 @@ int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_
   }
 }
 
+// ------------------------------------- pipelined tile step (fast FP32) --
+// Same tiles, same arithmetic and order as swe_tile_step_kernel<fast>, so
+// the result is bitwise the same; organised for GB300's latency and issue
+// limits instead of one CTA per tile:
+//   * persistent: one 512-thread CTA per SM walks tiles t, t + grid, ...;
+//   * the face geometry of the cells a thread owns (4 tile cells and 1 halo
+//     cell of level 1..3) is loaded into registers once per step and kept
+//     through the four stages (the stages touch shared memory only);
+//   * the next tile's state (own cells and halo) is copied into a second
+//     shared-memory buffer with cp.async while this tile computes, and its
+//     face records are prefetched into L2 with one bulk prefetch;
+//   * two tile cells are computed in lock step with the packed FP32x2
+//     instructions (__ffma2_rn, __fadd2_rn, __fmul2_rn: per lane the
+//     IEEE operations of the scalar kernel), halving the FP instructions;
+//   * stage states live in shared memory as three float arrays (h, uh, vh)
+//     at fixed offsets, so a neighbour's state is three 4-byte loads from
+//     one address register.
+namespace pipe {
+constexpr int kThreads = 512;
+constexpr int kOwn = 4;                     // tile cells per thread: n0 <= 2048
+constexpr int kMaxOwn = kOwn * kThreads;
+constexpr int kMaxLocal = 4096;             // nL
+constexpr int kBuf = 3 * kMaxLocal;         // floats of one (h, uh, vh) buffer
+constexpr int kSmemBytes = 4 * kBuf * 4;    // S0 x 2, SA, SB: 192 KB
+static_assert(kSmemBytes <= 227 * 1024, "shared memory of one CTA");
+
+struct Geo {  // one cell's three faces
+  float sx[3], sy[3], al[3];
+  int nb[3];
+};
+
+__device__ __forceinline__ void load_geo(const float4 *slot, int n3, int j, bool valid, Geo &g) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (valid) {
+      const float4 f = __ldg(slot + k * n3 + j);
+      g.sx[k] = f.x;
+      g.sy[k] = f.y;
+      g.al[k] = f.z;
+      g.nb[k] = __float_as_int(f.w);
+    } else {
+      g.sx[k] = g.sy[k] = g.al[k] = 0.f;
+      g.nb[k] = -2;
+    }
+  }
+}
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// a - b with one rounding (the product -1 * b is exact)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f, -1.f), a); }
+__device__ __forceinline__ float rcpf(float y) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+}
+
+// (h, uh, vh) arrays of one buffer at fixed offsets
+struct Buf {
+  float *p;
+  __device__ __forceinline__ float h(int j) const { return p[j]; }
+  __device__ __forceinline__ float u(int j) const { return p[kMaxLocal + j]; }
+  __device__ __forceinline__ float v(int j) const { return p[2 * kMaxLocal + j]; }
+  __device__ __forceinline__ void put(int j, float a, float b, float c) const {
+    p[j] = a;
+    p[kMaxLocal + j] = b;
+    p[2 * kMaxLocal + j] = c;
+  }
+};
+
+// One face of one cell, scalar (swe_tile_step_kernel's fast add_face / add_wall).
+__device__ __forceinline__ void face1(float &Sh, float &Su, float &Sv, float oh, float ou, float ov, const Buf &in,
+                                      int q, int nL, float a, float fx, float fy) {
+  if ((unsigned)q < (unsigned)nL) {
+    const float nh = in.h(q), nu = in.u(q), nv = in.v(q);
+    const float hf = fmaf(a, oh - nh, nh);
+    const float uhf = fmaf(a, ou - nu, nu);
+    const float vhf = fmaf(a, ov - nv, nv);
+    const float Fh = fmaf(uhf, fx, vhf * fy);
+    const float Fi = Fh * rcpf(hf);
+    const float hfs = (0.5f * hf) * hf;
+    Sh = Sh + Fh;
+    Su = fmaf(uhf, Fi, fmaf(hfs, fx, Su));
+    Sv = fmaf(vhf, Fi, fmaf(hfs, fy, Sv));
+  } else if (q == -1) {
+    const float gb = 0.5f * (oh * oh);
+    Su = fmaf(gb, fx, Su);
+    Sv = fmaf(gb, fy, Sv);
+  } else if (q >= 0) {  // corrupt layout: flag, never read outside the tile's list
+    esr::raise_status(ESR_DEV_IDX_RANGE);
+  }
+}
+
+// delta of two cells A, B (both lanes of every float2) from buffer `in`
+__device__ __forceinline__ void delta2(const Geo &gA, const Geo &gB, float2 oh, float2 ou, float2 ov, const Buf &in,
+                                       int nL, float2 &dh, float2 &du, float2 &dv) {
+  float2 Sh = f2(0.f, 0.f), Su = f2(0.f, 0.f), Sv = f2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int qA = gA.nb[k], qB = gB.nb[k];
+    if (((unsigned)qA < (unsigned)nL) & ((unsigned)qB < (unsigned)nL)) {
+      const float2 nh = f2(in.h(qA), in.h(qB));
+      const float2 nu = f2(in.u(qA), in.u(qB));
+      const float2 nv = f2(in.v(qA), in.v(qB));
+      const float2 a = f2(gA.al[k], gB.al[k]);
+      const float2 fx = f2(gA.sx[k], gB.sx[k]);
+      const float2 fy = f2(gA.sy[k], gB.sy[k]);
+      const float2 hf = fma2(a, sub2(oh, nh), nh);
+      const float2 uhf = fma2(a, sub2(ou, nu), nu);
+      const float2 vhf = fma2(a, sub2(ov, nv), nv);
+      const float2 Fh = fma2(uhf, fx, mul2(vhf, fy));
+      const float2 Fi = mul2(Fh, f2(rcpf(hf.x), rcpf(hf.y)));
+      const float2 hfs = mul2(mul2(f2(0.5f, 0.5f), hf), hf);
+      Sh = add2(Sh, Fh);
+      Su = fma2(uhf, Fi, fma2(hfs, fx, Su));
+      Sv = fma2(vhf, Fi, fma2(hfs, fy, Sv));
+    } else {
+      face1(Sh.x, Su.x, Sv.x, oh.x, ou.x, ov.x, in, qA, nL, gA.al[k], gA.sx[k], gA.sy[k]);
+      face1(Sh.y, Su.y, Sv.y, oh.y, ou.y, ov.y, in, qB, nL, gB.al[k], gB.sx[k], gB.sy[k]);
+    }
+  }
+  dh = f2(-Sh.x, -Sh.y);
+  du = f2(-Su.x, -Su.y);
+  dv = f2(-Sv.x, -Sv.y);
+}
+
+// 4-byte cp.async global -> shared
+__device__ __forceinline__ void cp4(float *dst, const float *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// state (h, uh, vh) of global cell g into buffer slot j
+__device__ __forceinline__ void fetch_state(const Buf &b, int j, const float4 *sin, int64_t g) {
+  const float *s = reinterpret_cast<const float *>(sin + g);
+  cp4(b.p + j, s);
+  cp4(b.p + kMaxLocal + j, s + 1);
+  cp4(b.p + 2 * kMaxLocal + j, s + 2);
+}
+
+struct TileMeta {
+  int cell_off, n0, n1, n2, n3, nL;
+  int64_t o3, oh;
+};
+
+__device__ __forceinline__ TileMeta tile_meta(const int32_t *meta, const int64_t *off3, const int64_t *offh, int t) {
+  const int32_t *m = meta + 8 * (int64_t)t;
+  return TileMeta{m[0], m[1], m[2], m[3], m[4], m[5], off3[t], offh[t]};
+}
+
+__device__ __forceinline__ bool tile_fits(const TileMeta &m, int64_t nc) {
+  return m.cell_off >= 0 && (int64_t)m.cell_off + m.n0 <= nc && m.n0 >= 0 && m.n0 <= kMaxOwn &&
+         m.nL <= kMaxLocal && m.n0 <= m.n1 && m.n1 <= m.n2 && m.n2 <= m.n3 && m.n3 <= m.nL;
+}
+
+// the own cells' state of tile m into buffer b (cp.async); the halo part
+// needs its indices first (fetch_halo)
+__device__ __forceinline__ void fetch_own(const Buf &b, const TileMeta &m, const float4 *sin) {
+  for (int j = threadIdx.x; j < m.n0; j += kThreads) fetch_state(b, j, sin, (int64_t)m.cell_off + j);
+}
+
+__device__ __forceinline__ void fetch_halo1(const Buf &b, int j, const float4 *sin, int64_t nc, int g) {
+  if (g < 0 || (int64_t)g >= nc) {  // corrupt layout: flag, never read out of bounds
+    esr::raise_status(ESR_DEV_IDX_RANGE);
+    b.put(j, 1.f, 0.f, 0.f);
+  } else {
+    fetch_state(b, j, sin, g);
+  }
+}
+
+// the halo's state: the first two cells of this thread from the indices
+// halo_index() loaded earlier, any further ones (large halos) index and copy
+// here
+__device__ __forceinline__ void fetch_halo(const Buf &b, const TileMeta &m, const float4 *sin, int64_t nc,
+                                           const int32_t *halo, const int (&hidx)[2]) {
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int j = m.n0 + threadIdx.x + r * kThreads;
+    if (j < m.nL) fetch_halo1(b, j, sin, nc, hidx[r]);
+  }
+  for (int j = m.n0 + threadIdx.x + 2 * kThreads; j < m.nL; j += kThreads)
+    fetch_halo1(b, j, sin, nc, __ldg(halo + m.oh + (j - m.n0)));
+}
+
+__device__ __forceinline__ void halo_index(const TileMeta &m, const int32_t *halo, int (&hidx)[2]) {
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int j = m.n0 + threadIdx.x + r * kThreads;
+    hidx[r] = j < m.nL ? __ldg(halo + m.oh + (j - m.n0)) : -1;
+  }
+}
+
+__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, Geo (&own)[kOwn], Geo &hal) {
+  const float4 *slot = gslot + 3 * m.o3;
+#pragma unroll
+  for (int r = 0; r < kOwn; ++r) {
+    const int j = threadIdx.x + r * kThreads;
+    load_geo(slot, m.n3, j, j < m.n0, own[r]);
+  }
+  const int jh = m.n0 + threadIdx.x;
+  load_geo(slot, m.n3, jh, jh < m.n3, hal);
+}
+
+// a halo cell (level 1..3): stage value only
+template <int STAGE>
+__device__ __forceinline__ void halo_cell(int j, const Geo &g, int nL, const Buf &in, const Buf &s0, const Buf &out,
+                                          float c) {
+  const float oh = in.h(j), ou = in.u(j), ov = in.v(j);
+  float Sh = 0.f, Su = 0.f, Sv = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) face1(Sh, Su, Sv, oh, ou, ov, in, g.nb[k], nL, g.al[k], g.sx[k], g.sy[k]);
+  const float h0 = STAGE == 1 ? oh : s0.h(j), u0 = STAGE == 1 ? ou : s0.u(j), v0 = STAGE == 1 ? ov : s0.v(j);
+  out.put(j, fmaf(c, -Sh, h0), fmaf(c, -Su, u0), fmaf(c, -Sv, v0));
+}
+
+// one stage on the tile's own cells (pairs r, r+1) and its halo cells
+template <int STAGE>
+__device__ __forceinline__ void stage(const TileMeta &m, const Geo (&own)[kOwn], const Geo &hal, const Buf &in,
+                                      const Buf &s0, const Buf &out, float2 (&acc)[kOwn / 2][3], float c,
+                                      float4 *sout, const float4 *gslot) {
+  const float2 c2 = f2(c, c);
+#pragma unroll
+  for (int p = 0; p < kOwn / 2; ++p) {
+    const int jA = threadIdx.x + 2 * p * kThreads;
+    const int jB0 = jA + kThreads;
+    if (jA >= m.n0) break;
+    const bool vB = jB0 < m.n0;
+    const int jB = vB ? jB0 : jA;
+    const float2 oh = f2(in.h(jA), in.h(jB)), ou = f2(in.u(jA), in.u(jB)), ov = f2(in.v(jA), in.v(jB));
+    float2 dh, du, dv;
+    delta2(own[2 * p], own[2 * p + 1], oh, ou, ov, in, m.nL, dh, du, dv);
+    const float2 h0 = STAGE == 1 ? oh : f2(s0.h(jA), s0.h(jB));
+    const float2 u0 = STAGE == 1 ? ou : f2(s0.u(jA), s0.u(jB));
+    const float2 v0 = STAGE == 1 ? ov : f2(s0.v(jA), s0.v(jB));
+    if (STAGE < 4) {
+      const float2 xh = fma2(c2, dh, h0), xu = fma2(c2, du, u0), xv = fma2(c2, dv, v0);
+      out.put(jA, xh.x, xu.x, xv.x);
+      if (vB) out.put(jB, xh.y, xu.y, xv.y);
+      if (STAGE == 1) {
+        acc[p][0] = dh;
+        acc[p][1] = du;
+        acc[p][2] = dv;
+      } else {
+        acc[p][0] = add2(acc[p][0], dh);
+        acc[p][1] = add2(acc[p][1], du);
+        acc[p][2] = add2(acc[p][2], dv);
+      }
+    } else {
+      const float2 xh = fma2(c2, add2(acc[p][0], dh), h0);
+      const float2 xu = fma2(c2, add2(acc[p][1], du), u0);
+      const float2 xv = fma2(c2, add2(acc[p][2], dv), v0);
+      sout[(int64_t)m.cell_off + jA] = make_float4(xh.x, xu.x, xv.x, 0.f);
+      if (vB) sout[(int64_t)m.cell_off + jB] = make_float4(xh.y, xu.y, xv.y, 0.f);
+    }
+  }
+  if (STAGE < 4) {  // halo cells whose level takes part in this stage
+    const int lim = STAGE == 1 ? m.n3 : STAGE == 2 ? m.n2 : m.n1;
+    int j = m.n0 + threadIdx.x;
+    if (j < lim) halo_cell<STAGE>(j, hal, m.nL, in, s0, out, c);
+    // more halo cells than threads (elongated tiles): face records from
+    // global memory (L1 / L2) in every stage
+    for (j += kThreads; j < lim; j += kThreads) {
+      Geo g;
+      load_geo(gslot + 3 * m.o3, m.n3, j, true, g);
+      halo_cell<STAGE>(j, g, m.nL, in, s0, out, c);
+    }
+  }
+}
+
+}  // namespace pipe
+
+__global__ void __launch_bounds__(pipe::kThreads, 1)
+swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
+                     const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
+                     const float4 *__restrict__ gslot, const float4 *__restrict__ sin, float4 *__restrict__ sout,
+                     int64_t nc, int ntiles, float c1, float c3, float c4) {
+  using namespace pipe;
+  extern __shared__ float smem[];
+  const Buf SA{smem + 2 * kBuf}, SB{smem + 3 * kBuf};
+  int t = blockIdx.x;
+  if (t >= ntiles) return;
+  TileMeta m = tile_meta(meta, off3, offh, t);
+  bool fits = tile_fits(m, nc);
+  int cur = 0;
+  Geo own[kOwn], hal;
+  int hidx[2];
+  if (fits) {  // prologue: the first tile's state and geometry
+    halo_index(m, halo, hidx);
+    fetch_own(Buf{smem}, m, sin);
+    fetch_halo(Buf{smem}, m, sin, nc, halo, hidx);
+    load_tile_geo(m, gslot, own, hal);
+  }
+  cp_commit();
+  while (true) {
+    const int tn = t + gridDim.x;
+    TileMeta mn{};
+    bool next = tn < ntiles;
+    if (next) {
+      mn = tile_meta(meta, off3, offh, tn);
+      if (!tile_fits(mn, nc)) {  // outside the kernel's limits: flag it, leave its cells unwritten
+        esr::raise_status(ESR_DEV_IDX_RANGE);
+      }
+    }
+    cp_wait_all();
+    __syncthreads();  // this tile's state is in buffer `cur`; the other buffer is free
+    const Buf S0{smem + cur * kBuf}, S0n{smem + (cur ^ 1) * kBuf};
+    const bool nfit = next && tile_fits(mn, nc);
+    if (nfit) {
+      if (threadIdx.x == 0) {  // the next tile's face records into L2
+        const float4 *g = gslot + 3 * mn.o3;
+        const unsigned bytes = (unsigned)(3 * (int64_t)mn.n3 * 16);
+        if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g), "r"(bytes) : "memory");
+      }
+      halo_index(mn, halo, hidx);
+      fetch_own(S0n, mn, sin);
+    }
+    if (fits) {
+      float2 acc[kOwn / 2][3];
+      stage<1>(m, own, hal, S0, S0, SA, acc, c1, sout, gslot);
+      if (nfit) fetch_halo(S0n, mn, sin, nc, halo, hidx);
+      cp_commit();
+      __syncthreads();
+      stage<2>(m, own, hal, SA, S0, SB, acc, c1, sout, gslot);
+      __syncthreads();
+      stage<3>(m, own, hal, SB, S0, SA, acc, c3, sout, gslot);
+      __syncthreads();
+      stage<4>(m, own, hal, SA, S0, SA, acc, c4, sout, gslot);
+    } else {
+      if (nfit) fetch_halo(S0n, mn, sin, nc, halo, hidx);
+      cp_commit();
+    }
+    if (!next) break;
+    // the next tile's geometry: this thread is done with the current one
+    if (nfit) load_tile_geo(mn, gslot, own, hal);
+    m = mn;
+    fits = nfit;
+    t = tn;
+    cur ^= 1;
+  }
+  cp_wait_all();
+}
+
+bool pipe_fits(const esr_swe_tiles *T) {
+  return !T->exact && T->max_own <= pipe::kMaxOwn && T->max_local <= pipe::kMaxLocal;
+}
+
+int run_pipe(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       pipe::kSmemBytes);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/pipelined smem attribute");
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/SM count");
+  const int grid = tiles->ntiles < sms ? tiles->ntiles : sms;
+  const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
+  float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
+  for (int64_t k = 0; k < steps; ++k) {
+    swe_tile_pipe_kernel<<<grid, pipe::kThreads, pipe::kSmemBytes, s>>>(
+        tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots, buf[k & 1],
+        buf[(k + 1) & 1], tiles->nc, tiles->ntiles, c1, c3, c4);
+  }
+  ESR_LAUNCH_CHECK("esr_swe_tile_step/pipelined");
+  return ESR_OK;
+}
+
 }  // namespace
 
 ESR_DEFINE_STATUS_READER(esr_status_swe)
@@ -658,15 +1028,32 @@ extern "C" int esr_swe_tile_threads(const esr_swe_tiles *tiles) {
   return tile_threads(tiles);
 }
 
-extern "C" int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
-                                 void *stream) {
+extern "C" int esr_swe_tile_kernel(const esr_swe_tiles *tiles) {
+  if (check_tiles(tiles)) return -1;
+  return pipe_fits(tiles) ? ESR_SWE_TILE_PIPELINED : ESR_SWE_TILE_BLOCKED;
+}
+
+extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, double dt, void *state_a,
+                                      void *state_b, int64_t steps, void *stream) {
   int st = check_tiles(tiles);
   if (st) return st;
   if (steps < 0) return esr::fail(ESR_ERR_ARG, "negative step count");
-  if (steps == 0) return ESR_OK;
   if (!state_a || !state_b || state_a == state_b) return esr::fail(ESR_ERR_ARG, "need two distinct state buffers");
   if (((uintptr_t)state_a | (uintptr_t)state_b) % 16) return esr::fail(ESR_ERR_ARG, "state buffers must be 16-byte aligned");
+  if (kernel == ESR_SWE_TILE_AUTO) kernel = pipe_fits(tiles) ? ESR_SWE_TILE_PIPELINED : ESR_SWE_TILE_BLOCKED;
+  if (kernel == ESR_SWE_TILE_PIPELINED && !pipe_fits(tiles))
+    return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, <= 2048 own cells and "
+                                          "<= 4096 local cells a tile");
+  if (kernel != ESR_SWE_TILE_PIPELINED && kernel != ESR_SWE_TILE_BLOCKED)
+    return esr::fail(ESR_ERR_ARG, "unknown tile kernel");
+  if (steps == 0) return ESR_OK;
   cudaStream_t s = esr::as_stream(stream);
+  if (kernel == ESR_SWE_TILE_PIPELINED) return run_pipe(tiles, dt, state_a, state_b, steps, s);
   return tiles->exact ? run_tiles<true>(tiles, dt, state_a, state_b, steps, s)
                       : run_tiles<false>(tiles, dt, state_a, state_b, steps, s);
+}
+
+extern "C" int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
+                                 void *stream) {
+  return esr_swe_tile_step_with(tiles, ESR_SWE_TILE_AUTO, dt, state_a, state_b, steps, stream);
 }

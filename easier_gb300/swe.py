@@ -60,6 +60,13 @@ DEFAULT_TILE_CELLS: Optional[int] = None
 TILE_MAX_L3 = 6144      # kernel limit on tile + 3 halo rings
 TILE_SMEM = 227 * 1024  # shared memory per CTA
 DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
+# Fast arithmetic on large meshes: tiles for the pipelined tile kernel
+# (<= 2048 own cells, <= 4096 local cells)
+PIPE_TILE_TARGET = 1900
+PIPE_LIMITS = dict(max_own=2048, max_local=4096)
+# tile kernel: "auto" (pipelined where the layout allows), "blocked" or "pipelined"
+DEFAULT_TILE_KERNEL = "auto"
+_TILE_KERNELS = {"auto": 0, "blocked": 1, "pipelined": 2}
 DEFAULT_PRECISION = "exact"  # "exact" (bitwise the reference) or "fast"
 # compile-time check of the fast arithmetic: one step from a random state,
 # max |fused - per-op| per component over max |h|
@@ -119,13 +126,19 @@ class SweEngine:
         self.nc = binding["nc"]
         self.tile_cells = min(tile_cells or DEFAULT_TILE_CELLS or self._auto_tile_cells(), TILE_CELLS)
         self.mode = mode
+        self.tile_kernel = DEFAULT_TILE_KERNEL
         self._build_layout()
 
     def _auto_tile_cells(self) -> int:
         """Largest tiles (least halo work) while there are enough of them to
         give every SM one."""
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count if self.device.type == "cuda" else 1
-        return max(TILE_MIN_CELLS, min(TILE_TARGET, -(-self.nc // sms)))
+        target = PIPE_TILE_TARGET if self.precision == "fast" else TILE_TARGET
+        return max(TILE_MIN_CELLS, min(target, -(-self.nc // sms)))
+
+    @staticmethod
+    def _pipe_fits(st: dict) -> bool:
+        return all(st[k] <= v for k, v in PIPE_LIMITS.items())
 
     # ----------------------------------------------------------- layout --
     def _build_layout(self) -> None:
@@ -137,6 +150,7 @@ class SweEngine:
         want_tiles = self.mode in ("tiled", "auto") and self.dtype == torch.float32
         tiles = None
         tile_cells = self.tile_cells
+        pipe_tries = 0
         while True:
             lay = cell_layout(nc, src, dst, bcell, reorder=self.reorder,
                               tile_cells=tile_cells if want_tiles else None)
@@ -145,7 +159,12 @@ class SweEngine:
             tiles = tile_layout(lay["nbr"], lay["part"])
             st = tiles["stats"]
             if st["max_own"] <= TILE_CELLS and st["max_l3"] <= TILE_MAX_L3 and st["smem"] <= TILE_SMEM:
-                break
+                # fast arithmetic: smaller tiles until the pipelined kernel takes them
+                if self.precision != "fast" or self._pipe_fits(st) or pipe_tries >= 4:
+                    break
+                pipe_tries += 1
+                tile_cells = max(TILE_MIN_CELLS, int(tile_cells * 0.85))
+                continue
             # halo too large for one CTA: smaller tiles, else the staged kernel
             tiles = None
             if tile_cells > 512:
@@ -226,10 +245,10 @@ class SweEngine:
             self.t_inv_area = self.inv_area[self.tile_area_src].contiguous()
             st = self.tile_stats
             self._tiles = _lib.SweTiles(self.nc, self.ntiles, _lib.F32, st["max_local"], st["max_l3"],
-                                        st["max_own"], 0, _lib.ptr(self.tile_meta), _lib.ptr(self.tile_off3),
-                                        _lib.ptr(self.tile_offh), _lib.ptr(self.tile_halo),
+                                        st["max_own"], st["max_halo3"], _lib.ptr(self.tile_meta),
+                                        _lib.ptr(self.tile_off3), _lib.ptr(self.tile_offh), _lib.ptr(self.tile_halo),
                                         _lib.ptr(self.t_slots), _lib.ptr(self.t_area), _lib.ptr(self.t_inv_area),
-                                        exact, 0)
+                                        exact, st["max_halo"])
 
     def set_precision(self, precision: str) -> None:
         """Switch between 'exact' and 'fast' arithmetic (same layout)."""
@@ -284,8 +303,8 @@ class SweEngine:
         stream = _lib.stream_handle(self.device)
         if self.tiled:
             a, b = self.bufs[self.cur], self.bufs[1 - self.cur]
-            _lib.call("esr_swe_tile_step", ctypes.byref(self._tiles), float(self.m.dt), _lib.ptr(a), _lib.ptr(b),
-                      int(steps), stream)
+            _lib.call("esr_swe_tile_step_with", ctypes.byref(self._tiles), _TILE_KERNELS[self.tile_kernel],
+                      float(self.m.dt), _lib.ptr(a), _lib.ptr(b), int(steps), stream)
             if steps % 2:
                 self.cur = 1 - self.cur
                 self._bind_views()
@@ -317,8 +336,17 @@ class SweEngine:
             st = self.tile_stats
             s += (f" tiles={st['ntiles']} own<={st['max_own']} L3/own={st['l3_over_own']:.3f}"
                   f" local/own={st['local_over_own']:.3f} smem={st['smem']}"
-                  f" cta={self.tile_threads()}")
+                  f" cta={self.tile_threads()} kernel={self.tile_kernel_name()}")
         return s
+
+    def tile_kernel_name(self) -> str:
+        """The tile kernel step() runs: 'pipelined' or 'blocked'."""
+        if not self.tiled:
+            return ""
+        k = _TILE_KERNELS[self.tile_kernel]
+        if k == 0:
+            k = int(_lib.lib().esr_swe_tile_kernel(ctypes.byref(self._tiles)))
+        return {1: "blocked", 2: "pipelined"}.get(k, "?")
 
     def touched_bytes_per_step(self) -> int:
         """HBM bytes one step must move in this layout, each array once."""
@@ -350,7 +378,7 @@ class SweEngine:
 
     def traffic_key(self) -> str:
         """Key of this kernel variant's measured DRAM bytes per launch."""
-        return f"swe_tiled_{self.precision}"
+        return f"swe_tiled_{self.tile_kernel_name()}_{self.precision}"
 
 
 def slot_width(nc: int, nd: np.ndarray, nb: np.ndarray) -> int:
@@ -452,6 +480,7 @@ def tile_layout(nbr: np.ndarray, part: np.ndarray) -> dict:
     cum = meta[:, 1:6].astype(np.int64)
     max_own, max_l3, max_local = int(cum[:, 0].max()), int(cum[:, 3].max()), int(cum[:, 4].max())
     stats = dict(ntiles=ntiles, max_own=max_own, max_l3=max_l3, max_local=max_local,
+                 max_halo3=int((cum[:, 3] - cum[:, 0]).max()), max_halo=int((cum[:, 4] - cum[:, 0]).max()),
                  mean_own=float(cum[:, 0].mean()), l3_over_own=float(t3.value / nc),
                  local_over_own=float(cum[:, 4].sum() / nc), smem=(3 * max_local + 6 * max_l3) * 4)
     return dict(meta=meta, off3=off3, offh=offh, halo=halo[:th.value], lnbr=lnbr, slot_src=slot_src,

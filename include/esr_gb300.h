@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 9
+#define ESR_GB300_ABI_VERSION 10
 
 /* element types */
 enum {
@@ -279,7 +279,7 @@ typedef struct {
   int32_t max_local; /* max nL */
   int32_t max_l3;    /* max n3 */
   int32_t max_own;   /* max n0 */
-  int32_t pad_;
+  int32_t max_halo3; /* max n3 - n0 (informational; not read) */
   const int32_t *meta;
   const int64_t *off3;
   const int64_t *offh;
@@ -288,7 +288,7 @@ typedef struct {
   const void *area;     /* [sum(n3)], read when exact != 0 */
   const void *inv_area; /* not read (reserved) */
   int32_t exact;        /* as in esr_swe_mesh */
-  int32_t pad2_;
+  int32_t max_halo;     /* max nL - n0 (informational; not read) */
 } esr_swe_tiles;
 
 /* Shared memory one CTA of esr_swe_tile_step uses, or -1 if the layout is
@@ -306,6 +306,31 @@ int esr_swe_tile_threads(const esr_swe_tiles *tiles);
  * `steps` is even, in state_b when odd. */
 int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
                       void *state_b, int64_t steps, void *stream);
+
+/* The two kernels behind esr_swe_tile_step, same results bit for bit:
+ *   BLOCKED: one CTA per tile (1024, 512 or 256 threads), the face records
+ *     read from global memory in every stage; any layout within the limits
+ *     above, exact or fast arithmetic;
+ *   PIPELINED: fast arithmetic only; one persistent 512-thread CTA per SM,
+ *     each thread's face records (4 tile cells, 1 halo cell) held in
+ *     registers through the four stages, the next tile's state copied into
+ *     shared memory (cp.async) and its records prefetched into L2 while the
+ *     current tile computes, two cells per thread in packed FP32x2
+ *     arithmetic.  Needs n0 <= 2048 and nL <= 4096 in every tile.
+ * AUTO picks PIPELINED when the layout allows it. */
+#define ESR_SWE_TILE_AUTO 0
+#define ESR_SWE_TILE_BLOCKED 1
+#define ESR_SWE_TILE_PIPELINED 2
+
+/* The kernel AUTO runs for this layout, or -1 if the layout is outside the
+ * limits.  No reference counterpart. */
+int esr_swe_tile_kernel(const esr_swe_tiles *tiles);
+
+/* esr_swe_tile_step on a chosen kernel (ESR_ERR_UNSUPPORTED if the layout
+ * does not fit it).  No reference counterpart. */
+int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, double dt,
+                           void *state_a, void *state_b, int64_t steps,
+                           void *stream);
 
 /* Host: partition an undirected graph (directed edge lists) into parts of at
  * most max_part vertices by recursive BFS bisection (compact parts; a set

@@ -204,3 +204,30 @@ def test_full_size_tiled_equals_staged_and_conserves_mass(monkeypatch):
         torch.cuda.empty_cache()
     for a, b in zip(*outs):
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("n,target", [(37, None), (150, 300), (300, None), (400, 700)])
+def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypatch):
+    """Fast arithmetic: the persistent pipelined tile kernel (state of the
+    next tile prefetched, geometry in registers, packed FP32x2 arithmetic)
+    is bitwise the one-CTA-per-tile kernel on the same layout, with one tile
+    per CTA (N=37, 150 without more tiles than SMs) and with CTAs walking
+    several tiles (more tiles than SMs)."""
+    from easier_gb300 import swe
+    if target:
+        monkeypatch.setattr(swe, "PIPE_TILE_TARGET", target)
+    eqn = workloads.make_swe(n, dt=5e-4, dtype=torch.float32)
+    [eqn] = esr.compile([eqn], "cuda", precision="fast")
+    eng = eqn.easier_fused_engine
+    assert eng.tiled and eng.tile_kernel_name() == "pipelined", eng.describe()
+    s0 = eng.state.clone()
+    outs = []
+    for kern in ("pipelined", "blocked"):
+        eng.tile_kernel = kern
+        eng.state.copy_(s0)
+        eng.step(7)
+        torch.cuda.synchronize()
+        outs.append(eng.state.clone())
+    from easier_gb300 import ops
+    assert ops.device_status() == 0
+    assert torch.equal(outs[0], outs[1])
