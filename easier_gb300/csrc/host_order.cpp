@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <exception>
 #include <string>
 #include <new>
 #include <system_error>
@@ -256,7 +257,6 @@ struct Bisector {
   int64_t *part;
   int64_t max_part;
   int par_depth;
-  std::atomic<bool> oom{false};  // a worker thread ran out of memory
 
   static int64_t ld(const int64_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
   static void st(int64_t *p, int64_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
@@ -316,26 +316,29 @@ struct Bisector {
     for (int64_t i = b; i < half; ++i) st(&label[verts[i]], ida);
     for (int64_t i = half; i < e; ++i) st(&label[verts[i]], idb);
     std::thread left;
+    std::exception_ptr err_left, err_right;  // whatever either half threw
     if (depth < par_depth) {
       try {
         left = std::thread([&] {
           try {
             run(b, half, ida, first_part, depth + 1);
-          } catch (const std::bad_alloc &) {
-            oom.store(true);
+          } catch (...) {
+            err_left = std::current_exception();
           }
         });
       } catch (const std::system_error &) {  // no thread to be had: this one does both halves
       }
     }
     if (left.joinable()) {
+      // the worker is always joined before anything leaves this scope
       try {
         run(half, e, idb, first_part + k / 2, depth + 1);
-      } catch (const std::bad_alloc &) {
-        oom.store(true);
+      } catch (...) {
+        err_right = std::current_exception();
       }
       left.join();
-      if (oom.load()) throw std::bad_alloc();
+      if (err_left) std::rethrow_exception(err_left);
+      if (err_right) std::rethrow_exception(err_right);
     } else {
       run(b, half, ida, first_part, depth + 1);
       run(half, e, idb, first_part + k / 2, depth + 1);
@@ -352,6 +355,7 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
   for (int64_t e = 0; e < m; ++e)
     if (src[e] < 0 || src[e] >= n || dst[e] < 0 || dst[e] >= n)
       return esr::fail(ESR_ERR_ARG, "edge endpoint out of range");
+  ESR_HOST_TRY
   std::vector<int64_t> ptr(n + 1, 0);
   for (int64_t e = 0; e < m; ++e) {
     if (src[e] == dst[e]) continue;
@@ -374,14 +378,11 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   int par_depth = 0;
   while ((1u << par_depth) < 2 * hw && par_depth < 8) ++par_depth;
-  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth, {}};
-  try {
-    if (n > 0) bs.run(0, n, 0, 0, 0);
-  } catch (const std::bad_alloc &) {
-    return esr::fail(ESR_ERR_ARG, "out of host memory");
-  }
+  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth};
+  if (n > 0) bs.run(0, n, 0, 0, 0);
   *nparts = n > 0 ? (n + max_part - 1) / max_part : 0;
   return ESR_OK;
+  ESR_HOST_CATCH
 }
 
 

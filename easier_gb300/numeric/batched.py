@@ -76,7 +76,8 @@ class PackedBatch:
     whose Ae is exactly 0 are left out: they add exactly nothing to a row's
     sum of finite products (P1 grids: the hypotenuse couplings of right
     triangles, a third of all), so the SpMV moves and multiplies less for
-    the same result.  The GNN's message passing keeps them as graph edges."""
+    the same result (for finite vectors: the reference's 0 * Inf = NaN is
+    not reproduced).  The GNN's message passing keeps them as graph edges."""
 
     def __init__(self, instances: Sequence[LinsysInstance], edge_features: bool = False):
         if len(instances) == 0:
@@ -161,6 +162,14 @@ def chunk_layout(inst_block0: np.ndarray, tiles_per_chunk: int):
     return chunk_tile0.astype(np.int32), chunk_inst.astype(np.int32), inst_chunk0.astype(np.int32)
 
 
+# Iterations between the GNN stall checks (no decrease of r.r over the
+# window, or the network's correction cut in more than half of it -> the
+# instance falls back to Jacobi-PCG).  Where the network does not help, the
+# first check decides; a short window keeps the failed GNN iterations (each
+# costing several Jacobi iterations) few.
+GNN_STALL_WINDOW = 16
+
+
 class BatchedPCG:
     """Lockstep (P)CG over a packed batch on one GPU.
 
@@ -173,7 +182,7 @@ class BatchedPCG:
 
     def __init__(self, instances: Sequence[LinsysInstance], jacobi: bool = True, precision: str = "df64",
                  device="cuda", graph_iters: int = 32, use_graph: bool = True, tiles_per_chunk: int = 4,
-                 grid: Optional[int] = None, gnn=None, stall_window: int = 64, gnn_ctas_per_sm: int = 2):
+                 grid: Optional[int] = None, gnn=None, stall_window: int = None, gnn_ctas_per_sm: int = 2):
         if precision not in ("fp64", "df64"):
             raise ValueError("precision must be 'fp64' or 'df64'")
         dev = torch.device(device)
@@ -229,7 +238,8 @@ class BatchedPCG:
             self.gnn_desc = _lib.Gnn(_lib.ptr(g["node_lk"]), _lib.ptr(g["edge_feat"]), _lib.ptr(g["inst_rows"]),
                                      _lib.ptr(g["h0"]), _lib.ptr(g["h1"]), _lib.ptr(g["enc_w"]), _lib.ptr(g["enc_b"]),
                                      _lib.ptr(g["layer_w"]), _lib.ptr(g["layer_b"]), _lib.ptr(g["dec_w"]),
-                                     float(gnn.dec_b), int(gnn_ctas_per_sm * self.sm_count), int(stall_window), 0)
+                                     float(gnn.dec_b), int(gnn_ctas_per_sm * self.sm_count),
+                                     int(GNN_STALL_WINDOW if stall_window is None else stall_window), 0)
         self.set_shape(tiles_per_chunk, grid if grid is not None else 4 * self.sm_count)
 
     def set_shape(self, tiles_per_chunk: int, grid: int):

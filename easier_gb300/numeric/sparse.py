@@ -56,7 +56,12 @@ class SellMatrix:
     def from_linsys(cls, A, dtype: Optional[torch.dtype] = None) -> "SellMatrix":
         """The Linsys's current values; couplings whose Ae is exactly 0 are
         left out (they add exactly nothing to a row's sum of finite
-        products; the solvers rebuild their plan when Ae changes)."""
+        products; the solvers rebuild their plan when Ae changes).  For a
+        vector x with an Inf or NaN the results differ from the
+        reference's reducer(selector(x) * Ae), where 0 * Inf gives NaN:
+        the packed SpMV is the reference's Linsys for finite x only (a
+        solver that meets a non-finite value stops with a breakdown
+        status either way)."""
         sel, red = A.selector, A.reducer
         n = A.Av.shape[0]
         if red.n != n:

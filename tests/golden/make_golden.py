@@ -12,7 +12,8 @@ OpenMP is pinned to one thread: the reference mesh generator writes shared
 corner points from several loop iterations, so with more threads their last
 bit depends on timing.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [group ...]   (groups: mesh,
+        selector_reducer, poisson, poisson_fv_n100, linsys_p1, swe; default all)
 Writes: tests/golden/*.npz (small; committed).
 """
 import os
@@ -162,6 +163,25 @@ def poisson_fixtures():
     np.savez_compressed(HERE / "poisson_fv_n10_solve.npz", **out)
 
 
+def poisson_fv_n100_fixture():
+    """The tutorial's FV Poisson at N=100 (40,000 cells, 119,600 directed
+    edges) solved by the reference's CG (no preconditioner, as the tutorial
+    does) to relative residual 1e-8."""
+    n = 100
+    mp = put_mesh(n)
+    pp = f"poisson{n}"
+    assemble_poisson(mp, pp)
+    eqn = Poisson(mp, pp)
+    sol = CG(eqn.A, eqn.b, eqn.x)
+    [eqn, sol] = esr.compile([eqn, sol], "cpu", partition_mode="evenly")
+    t0 = time.time()
+    info = sol.solve(rtol=1e-8, maxiter=5000)
+    out = {"cg_x": eqn.x.collect().numpy(), "cg_iters": np.array(info["iters"]),
+           "cg_residual": np.array(info["residual"]), "b": eqn.b.collect().numpy()}
+    np.savez_compressed(HERE / "poisson_fv_n100_cg.npz", **out)
+    print(f"poisson fv n100: {info['iters']} CG iterations in {time.time() - t0:.1f} s")
+
+
 def linsys_p1_fixture():
     """The reference's Linsys + CG on a P1 system given as arrays (no
     reference assembly exists for P1; the arrays come from a plain numpy
@@ -237,11 +257,12 @@ def selector_reducer_fixture():
     np.savez_compressed(HERE / "selector_reducer.npz", **out)
 
 
+GROUPS = {"mesh": mesh_fixtures, "selector_reducer": selector_reducer_fixture, "poisson": poisson_fixtures,
+          "poisson_fv_n100": poisson_fv_n100_fixture, "linsys_p1": linsys_p1_fixture, "swe": swe_fixtures}
+
 if __name__ == "__main__":
+    # python tests/golden/make_golden.py [group ...]  (default: all groups)
     t0 = time.time()
-    mesh_fixtures()
-    selector_reducer_fixture()
-    poisson_fixtures()
-    linsys_p1_fixture()
-    swe_fixtures()
+    for name in (sys.argv[1:] or list(GROUPS)):
+        GROUPS[name]()
     print(f"golden fixtures written in {time.time() - t0:.0f} s")
