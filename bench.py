@@ -12,6 +12,10 @@ Workloads (``--workload``):
            couplings), random-mode RHS, Jacobi-PCG to relative residual 1e-8;
            one bench step = one solve; metric solves/s
            (``--precision native|mixed|df64``).
+  poisson-fv  the tutorial's cell-centred FV Poisson (tutorial/poisson) on
+           the tutorial mesh, N=500 (1,000,000 cells, 2,998,000 directed
+           edges), CG without a preconditioner as the tutorial runs it, to
+           relative residual 1e-8; metric solves/s.
   batched  256 P1 Poisson instances, side N ~ U{32..512} (seeded), GRF
            kappa, random-mode RHS, packed block-diagonal, lockstep
            Jacobi-PCG per instance to FP64-verified relative residual 1e-8;
@@ -147,6 +151,13 @@ def swe_config(args, world):
 
 
 def poisson_config(args, world):
+    if args.workload == "poisson-fv":
+        nc, ne, _ = swe_sizes(args.n)
+        return {"workload": f"FV Poisson (the tutorial's), tutorial mesh N={args.n} ({nc} cells, {ne} directed "
+                            f"edges), CG without preconditioner to FP64 true rel. residual 1e-8",
+                "unknowns": nc, "precision": args.precision, "parallelism": f"replicas x{world}",
+                "l2": "working set larger than L2 (matrix + 6 vectors)" if nc >= 1_000_000 else
+                      "working set smaller than L2"}
     return {"workload": f"P1 Poisson {args.n}x{args.n} grid, 16 random sine modes (seed 0), Jacobi-PCG to FP64 "
                         f"true rel. residual 1e-8",
             "unknowns": (args.n - 1) ** 2, "precision": args.precision, "parallelism": f"replicas x{world}",
@@ -393,8 +404,13 @@ def bench_poisson(args, world, rank, local):
     from easier_gb300.numeric.solver import CG
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    eqn = workloads.P1Poisson(args.n, rhs_seed=0)
-    sol = CG(eqn.A, eqn.b, eqn.x, M=Jacobi(eqn.A))
+    fv = args.workload == "poisson-fv"
+    if fv:  # the tutorial's FV Poisson and its solver call: CG without a preconditioner
+        eqn = workloads.make_poisson_fv(args.n)
+        sol = CG(eqn.A, eqn.b, eqn.x)
+    else:
+        eqn = workloads.P1Poisson(args.n, rhs_seed=0)
+        sol = CG(eqn.A, eqn.b, eqn.x, M=Jacobi(eqn.A))
     [eqn, sol] = esr.compile([eqn, sol], "cuda")
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
@@ -434,7 +450,8 @@ def bench_poisson(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": dtype,
-        "data": "synthetic (16 random sine modes, seed 0)",
+        "data": ("tutorial FV Poisson right hand side (Gaussian source)" if fv else
+                 "synthetic (16 random sine modes, seed 0)"),
         "config": poisson_config(args, world),
         "solve": {"couplings": int(eqn.selector.idx.numel()), "iterations": nit, "bytes_per_iteration": bytes_it,
                   "replacements": info.get("restarts", info.get("replacements")), "true_rel_residual": rel},
@@ -463,20 +480,31 @@ def bench_poisson(args, world, rank, local):
     line["e2e"] = {"value": world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                    "path": "CG.solve on the compiled module, b in and x out through pinned host memory"}
     if rank == 0 and not args.no_cpu_baseline:
-        from easier_gb300 import mesh
         from oracle import cg as ocg
-        s = mesh.p1_system(args.n)
-        bb = mesh.random_mode_rhs(args.n, 0)
+        row, col, Ae, Av, bb = _poisson_arrays(args, eqn)
         k = 40
         t0 = time.perf_counter()
-        ocg.cg(s.row, s.col, s.Ae, s.Av, bb, rtol=0.0, maxiter=k - 1, jacobi=True)
+        ocg.cg(row, col, Ae, Av, bb, rtol=0.0, maxiter=k - 1, jacobi=not fv)
         per_it = (time.perf_counter() - t0) / k
+        what = f"FV Poisson N={args.n} CG" if fv else f"{args.n}x{args.n} P1 Jacobi-PCG"
         line["cpu_baseline"] = {"value": 1.0 / (per_it * (nit + 1)), "unit": "solves/s",
                                 "cores": torch.get_num_threads(), "kind": "port",
-                                "sample": f"{k} oracle Jacobi-PCG iterations on the {args.n}x{args.n} P1 system "
+                                "sample": f"{k} oracle iterations of the {what} system "
                                           f"({per_it * 1e3:.1f} ms each), scaled to the {nit:.0f} iterations of a "
                                           f"solve"}
     return line
+
+
+def _poisson_arrays(args, eqn):
+    """(row, col, Ae, Av, b) of the workload's system for the oracle (host
+    numpy, the generators' order)."""
+    from easier_gb300 import mesh
+    if args.workload == "poisson-fv":
+        m = mesh.triangular_mesh(args.n)
+        a = mesh.poisson_fv(m)
+        return m.src, m.dst, a.Af, a.Ac, a.b
+    s = mesh.p1_system(args.n)
+    return s.row, s.col, s.Ae, s.Av, mesh.random_mode_rhs(args.n, 0)
 
 
 # -------------------------------------------------------- batched Poisson --
@@ -704,6 +732,7 @@ def bench_gnn(args, world, rank, local):
 def solver_secondaries(args, world, rank, local):
     """The solver workloads, each bounded, on the default SWE line:
     P1-1000 Jacobi-PCG in FP64 and double-float (3 timed solves each), the
+    tutorial's FV Poisson at N=500 with its CG (3 timed solves), the
     256-instance batch in double-float (one timed one-launch batch solve)
     and GNN flexible CG against Jacobi-PCG on the held-out batch (one timed
     batch each).  Each keeps its own CUDA-event timing, FP64-verified
@@ -714,6 +743,8 @@ def solver_secondaries(args, world, rank, local):
                                                           warmup=1, seed=0)),
             ("poisson_p1_1000_df64", bench_poisson, dict(workload="poisson", n=1000, precision="df64", steps=3,
                                                           warmup=1, seed=0)),
+            ("poisson_fv_500_fp64", bench_poisson, dict(workload="poisson-fv", n=500, precision="native", steps=3,
+                                                         warmup=1, seed=0)),
             ("batched_256_df64", bench_batched, dict(workload="batched", precision="df64", steps=1, warmup=1,
                                                       seed=0)),
             ("gnn_vs_jacobi_256_heldout", bench_gnn, dict(workload="gnn", precision="df64", steps=1, warmup=1,
@@ -722,11 +753,13 @@ def solver_secondaries(args, world, rank, local):
         a = copy.copy(args)
         for k, v in over.items():
             setattr(a, k, v)
-        a.no_cpu_baseline = True
+        # CPU baselines only where a bounded sample costs seconds (the
+        # single-system solves: 40 oracle iterations)
+        a.no_cpu_baseline = args.no_cpu_baseline or fn is not bench_poisson
         t0 = time.perf_counter()
         line = fn(a, world, rank, local)
         keep = {k: line[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "dtype", "config", "solve",
-                                     "roofline", "e2e", "gpu_launches", "clocks") if k in line}
+                                     "roofline", "e2e", "gpu_launches", "clocks", "cpu_baseline") if k in line}
         keep["wall_s"] = time.perf_counter() - t0
         out[name] = keep
         torch.cuda.empty_cache()
@@ -822,20 +855,27 @@ def bench_reference(args, world):
                   f"(N={sizes}), one per step (instance assembly not timed)")
         cfg = batched_config(args, world)
     else:
-        from easier_gb300 import mesh as gen
-        row, col, Ae, Av = omesh.p1_arrays(args.n)
-        b = gen.random_mode_rhs(args.n, 0)
+        fv = args.workload == "poisson-fv"
+        if fv:  # the tutorial's FV Poisson, CG without a preconditioner as the tutorial runs it
+            m = omesh.triangular_mesh(args.n)
+            a = omesh.poisson_fv(m)
+            row, col, Ae, Av, b = m["src"], m["dst"], a["Af"], a["Ac"], a["b"]
+        else:
+            from easier_gb300 import mesh as gen
+            row, col, Ae, Av = omesh.p1_arrays(args.n)
+            b = gen.random_mode_rhs(args.n, 0)
         setup = time.perf_counter() - t_setup
         for _ in range(args.warmup):
-            ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)
+            ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=not fv)
         its = []
 
         def one(_):
-            its.append(ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=True)[1])
+            its.append(ocg.cg(row, col, Ae, Av, b, rtol=1e-8, jacobi=not fv)[1])
         args.steps, wall = _bounded(one, requested)
         v = args.steps / wall
         unit, metric = "solves/s", "Poisson solves/s"
-        sample = f"{args.steps} full Jacobi-PCG solves ({its[-1]} iterations each) on the {args.n}x{args.n} P1 grid"
+        sample = (f"{args.steps} full CG solves ({its[-1]} iterations each) of the FV Poisson at N={args.n}" if fv else
+                  f"{args.steps} full Jacobi-PCG solves ({its[-1]} iterations each) on the {args.n}x{args.n} P1 grid")
         cfg = poisson_config(args, world)
     cores = torch.get_num_threads()
     if args.steps < requested:
@@ -855,7 +895,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["swe", "poisson", "batched", "gnn"], default="swe")
+    ap.add_argument("--workload", choices=["swe", "poisson", "poisson-fv", "batched", "gnn"], default="swe")
     ap.add_argument("--count", type=int, default=256, help="batched: instances")
     ap.add_argument("--nmin", type=int, default=32, help="batched: smallest mesh side")
     ap.add_argument("--nmax", type=int, default=512, help="batched: largest mesh side")
@@ -875,7 +915,7 @@ def main():
     ap.add_argument("--tile-cells", type=int, default=None, help="swe: target cells per tile (FP32 tiled step)")
     args = ap.parse_args()
     if args.n is None:
-        args.n = 2000 if args.workload == "swe" else 1000
+        args.n = {"swe": 2000, "poisson-fv": 500}.get(args.workload, 1000)
     if args.dt is None:
         # dt = 5e-4 at N=2000 exceeds the scheme's stability limit (the state
         # turns non-finite within ~200 steps); 2.5e-4 is stable for 1000+
@@ -888,15 +928,15 @@ def main():
     world, rank, local = _dist()
     if args.impl == "reference":
         if args.steps is None:
-            args.steps = {"swe": 3, "poisson": 1, "batched": 4, "gnn": 4}[args.workload]
+            args.steps = {"swe": 3, "poisson": 1, "poisson-fv": 2, "batched": 4, "gnn": 4}[args.workload]
         if args.warmup is None:
-            args.warmup = {"swe": 1, "poisson": 0, "batched": 1, "gnn": 1}[args.workload]
+            args.warmup = {"swe": 1, "poisson": 0, "poisson-fv": 0, "batched": 1, "gnn": 1}[args.workload]
         if rank != 0:
             return
         print(json.dumps(bench_reference(args, world)), flush=True)
         return
     if args.steps is None:
-        args.steps = {"swe": 1000, "poisson": 10, "batched": 5, "gnn": 3}[args.workload]
+        args.steps = {"swe": 1000, "poisson": 10, "poisson-fv": 10, "batched": 5, "gnn": 3}[args.workload]
     if args.warmup is None:
         args.warmup = 10 if args.workload == "swe" else 3
     if args.warmup < 3:
@@ -904,7 +944,8 @@ def main():
     if world > 1:
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    run = {"swe": bench_swe, "poisson": bench_poisson, "batched": bench_batched, "gnn": bench_gnn}[args.workload]
+    run = {"swe": bench_swe, "poisson": bench_poisson, "poisson-fv": bench_poisson, "batched": bench_batched,
+           "gnn": bench_gnn}[args.workload]
     line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -93,6 +93,9 @@ _SIGS = {
     "esr_mesh_triangular": (c_int, [c_int64, _P, _P, _P, _P, _P, _P]),
     "esr_swe_geometry": (c_int, [c_int64, c_int64, c_int64] + [_P] * 14),
     "esr_poisson_fv_assemble": (c_int, [c_int64, c_int64, c_int64] + [_P] * 11),
+    "esr_mesh_triangular_device": (c_int, [c_int64] + [_P] * 7),
+    "esr_swe_geometry_device": (c_int, [c_int64, c_int64, c_int64, c_int64] + [_P] * 15),
+    "esr_poisson_fv_assemble_device": (c_int, [c_int64, c_int64, c_int64, c_int64] + [_P] * 16),
     "esr_p1_sizes": (c_int, [c_int64, POINTER(c_int64), POINTER(c_int64)]),
     "esr_p1_assemble": (c_int, [c_int64, _P, _P, _P, _P, _P]),
     "esr_csr_from_index": (c_int, [_P, c_int64, c_int64, _P, _P]),

@@ -10,6 +10,7 @@ int esr_status_gather_reduce(int *bits, int clear, cudaStream_t s);
 int esr_status_swe(int *bits, int clear, cudaStream_t s);
 int esr_status_cg(int *bits, int clear, cudaStream_t s);
 int esr_status_gnn(int *bits, int clear, cudaStream_t s);
+int esr_status_mesh_gpu(int *bits, int clear, cudaStream_t s);
 
 namespace esr {
 int cuda_check(cudaError_t e, const char *where) {
@@ -27,6 +28,7 @@ extern "C" int esr_device_status(int *status_out, int clear, void *stream) {
   if ((st = esr_status_swe(&bits, clear, s))) return st;
   if ((st = esr_status_cg(&bits, clear, s))) return st;
   if ((st = esr_status_gnn(&bits, clear, s))) return st;
+  if ((st = esr_status_mesh_gpu(&bits, clear, s))) return st;
   if ((st = esr_status_runtime(&bits, clear, s))) return st;
   *status_out = bits;
   return ESR_OK;

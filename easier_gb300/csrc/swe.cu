@@ -704,20 +704,42 @@ __device__ __forceinline__ void face1(float &Sh, float &Su, float &Sv, float oh,
   }
 }
 
+// Face records of two tile cells A, B, held as the lanes of float2 values
+// so the packed arithmetic takes them without re-pairing registers in
+// every stage.
+struct GeoPair {
+  float2 sx[3], sy[3], al[3];
+  int nbA[3], nbB[3];
+};
+
+__device__ __forceinline__ void load_pair(const float4 *slot, int n3, int jA, bool vA, int jB, bool vB, GeoPair &g) {
+  Geo a, b;
+  load_geo(slot, n3, jA, vA, a);
+  load_geo(slot, n3, jB, vB, b);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    g.sx[k] = f2(a.sx[k], b.sx[k]);
+    g.sy[k] = f2(a.sy[k], b.sy[k]);
+    g.al[k] = f2(a.al[k], b.al[k]);
+    g.nbA[k] = a.nb[k];
+    g.nbB[k] = b.nb[k];
+  }
+}
+
 // delta of two cells A, B (both lanes of every float2) from buffer `in`
-__device__ __forceinline__ void delta2(const Geo &gA, const Geo &gB, float2 oh, float2 ou, float2 ov, const Buf &in,
+__device__ __forceinline__ void delta2(const GeoPair &g, float2 oh, float2 ou, float2 ov, const Buf &in,
                                        int nL, float2 &dh, float2 &du, float2 &dv) {
   float2 Sh = f2(0.f, 0.f), Su = f2(0.f, 0.f), Sv = f2(0.f, 0.f);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const int qA = gA.nb[k], qB = gB.nb[k];
+    const int qA = g.nbA[k], qB = g.nbB[k];
     if (((unsigned)qA < (unsigned)nL) & ((unsigned)qB < (unsigned)nL)) {
       const float2 nh = f2(in.h(qA), in.h(qB));
       const float2 nu = f2(in.u(qA), in.u(qB));
       const float2 nv = f2(in.v(qA), in.v(qB));
-      const float2 a = f2(gA.al[k], gB.al[k]);
-      const float2 fx = f2(gA.sx[k], gB.sx[k]);
-      const float2 fy = f2(gA.sy[k], gB.sy[k]);
+      const float2 a = g.al[k];
+      const float2 fx = g.sx[k];
+      const float2 fy = g.sy[k];
       const float2 hf = fma2(a, sub2(oh, nh), nh);
       const float2 uhf = fma2(a, sub2(ou, nu), nu);
       const float2 vhf = fma2(a, sub2(ov, nv), nv);
@@ -728,8 +750,8 @@ __device__ __forceinline__ void delta2(const Geo &gA, const Geo &gB, float2 oh, 
       Su = fma2(uhf, Fi, fma2(hfs, fx, Su));
       Sv = fma2(vhf, Fi, fma2(hfs, fy, Sv));
     } else {
-      face1(Sh.x, Su.x, Sv.x, oh.x, ou.x, ov.x, in, qA, nL, gA.al[k], gA.sx[k], gA.sy[k]);
-      face1(Sh.y, Su.y, Sv.y, oh.y, ou.y, ov.y, in, qB, nL, gB.al[k], gB.sx[k], gB.sy[k]);
+      face1(Sh.x, Su.x, Sv.x, oh.x, ou.x, ov.x, in, qA, nL, g.al[k].x, g.sx[k].x, g.sy[k].x);
+      face1(Sh.y, Su.y, Sv.y, oh.y, ou.y, ov.y, in, qB, nL, g.al[k].y, g.sx[k].y, g.sy[k].y);
     }
   }
   dh = f2(-Sh.x, -Sh.y);
@@ -805,12 +827,13 @@ __device__ __forceinline__ void halo_index(const TileMeta &m, const int32_t *hal
   }
 }
 
-__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, Geo (&own)[kOwn], Geo &hal) {
+__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, GeoPair (&own)[kOwn / 2],
+                                              Geo &hal) {
   const float4 *slot = gslot + 3 * m.o3;
 #pragma unroll
-  for (int r = 0; r < kOwn; ++r) {
-    const int j = threadIdx.x + r * kThreads;
-    load_geo(slot, m.n3, j, j < m.n0, own[r]);
+  for (int p = 0; p < kOwn / 2; ++p) {
+    const int jA = threadIdx.x + 2 * p * kThreads, jB = jA + kThreads;
+    load_pair(slot, m.n3, jA, jA < m.n0, jB, jB < m.n0, own[p]);
   }
   const int jh = m.n0 + threadIdx.x;
   load_geo(slot, m.n3, jh, jh < m.n3, hal);
@@ -830,7 +853,7 @@ __device__ __forceinline__ void halo_cell(int j, const Geo &g, int nL, const Buf
 
 // one stage on the tile's own cells (pairs r, r+1) and its halo cells
 template <int STAGE>
-__device__ __forceinline__ void stage(const TileMeta &m, const Geo (&own)[kOwn], const Geo &hal, const Buf &in,
+__device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[kOwn / 2], const Geo &hal, const Buf &in,
                                       const Buf &s0, const Buf &out, float2 (&acc)[kOwn / 2][3], float c,
                                       float4 *sout, const float4 *gslot) {
   const float2 c2 = f2(c, c);
@@ -843,7 +866,7 @@ __device__ __forceinline__ void stage(const TileMeta &m, const Geo (&own)[kOwn],
     const int jB = vB ? jB0 : jA;
     const float2 oh = f2(in.h(jA), in.h(jB)), ou = f2(in.u(jA), in.u(jB)), ov = f2(in.v(jA), in.v(jB));
     float2 dh, du, dv;
-    delta2(own[2 * p], own[2 * p + 1], oh, ou, ov, in, m.nL, dh, du, dv);
+    delta2(own[p], oh, ou, ov, in, m.nL, dh, du, dv);
     const float2 h0 = STAGE == 1 ? oh : f2(s0.h(jA), s0.h(jB));
     const float2 u0 = STAGE == 1 ? ou : f2(s0.u(jA), s0.u(jB));
     const float2 v0 = STAGE == 1 ? ov : f2(s0.v(jA), s0.v(jB));
@@ -897,7 +920,8 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   TileMeta m = tile_meta(meta, off3, offh, t);
   bool fits = tile_fits(m, nc);
   int cur = 0;
-  Geo own[kOwn], hal;
+  GeoPair own[kOwn / 2];
+  Geo hal;
   int hidx[2];
   if (fits) {  // prologue: the first tile's state and geometry
     halo_index(m, halo, hidx);

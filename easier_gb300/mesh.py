@@ -13,6 +13,7 @@ from dataclasses import dataclass
 from typing import Optional
 
 import numpy as np
+import torch
 
 from . import _lib
 
@@ -55,9 +56,24 @@ def mesh_sizes(n: int):
     return tuple(o.value for o in out)
 
 
-def triangular_mesh(n: int) -> TriangularMesh:
-    """Same arrays as the reference's ``generate_triangular_mesh(n)``."""
+def _on_cuda(mesh) -> bool:
+    return isinstance(mesh.src, torch.Tensor) and mesh.src.is_cuda
+
+
+def triangular_mesh(n: int, device=None) -> TriangularMesh:
+    """Same arrays as the reference's ``generate_triangular_mesh(n)``.  With
+    a CUDA ``device`` the mesh is generated there (esr_mesh_triangular_device,
+    bitwise the host generator's) and the fields are device tensors."""
     nc, ne, nbc, npts = mesh_sizes(n)
+    if device is not None and torch.device(device).type == "cuda":
+        dev = torch.device(device)
+        i64 = dict(dtype=torch.int64, device=dev)
+        m = TriangularMesh(n, torch.empty(ne, **i64), torch.empty(ne, **i64), torch.empty((nc, 3), **i64),
+                           torch.empty(nbc, **i64), torch.empty((nbc, 2), **i64),
+                           torch.empty((npts, 2), dtype=torch.float64, device=dev))
+        _lib.call("esr_mesh_triangular_device", n, _lib.ptr(m.src), _lib.ptr(m.dst), _lib.ptr(m.cells),
+                  _lib.ptr(m.bcells), _lib.ptr(m.bpoints), _lib.ptr(m.points), _lib.stream_handle(dev))
+        return m
     src = np.empty(ne, np.int64)
     dst = np.empty(ne, np.int64)
     cells = np.empty((nc, 3), np.int64)
@@ -83,7 +99,17 @@ class SweGeometry:
 
 
 def swe_geometry(mesh: TriangularMesh) -> SweGeometry:
+    """assemble_shallow_water.py:154-253; a mesh of CUDA tensors is
+    assembled on its device (esr_swe_geometry_device, bitwise the host's)."""
     nc, ne, nbc = mesh.nc, mesh.ne, mesh.nbc
+    if _on_cuda(mesh):
+        dev = mesh.src.device
+        g = SweGeometry(*(torch.empty(k, dtype=torch.float64, device=dev) for k in (ne, ne, ne, nc, nc, nc, nbc, nbc)))
+        _lib.call("esr_swe_geometry_device", nc, ne, nbc, mesh.points.shape[0], _lib.ptr(mesh.src),
+                  _lib.ptr(mesh.dst), _lib.ptr(mesh.cells), _lib.ptr(mesh.bcells), _lib.ptr(mesh.bpoints),
+                  _lib.ptr(mesh.points), _lib.ptr(g.sx), _lib.ptr(g.sy), _lib.ptr(g.alpha), _lib.ptr(g.area),
+                  _lib.ptr(g.x), _lib.ptr(g.y), _lib.ptr(g.bsx), _lib.ptr(g.bsy), _lib.stream_handle(dev))
+        return g
     g = SweGeometry(*(np.empty(k, np.float64) for k in (ne, ne, ne, nc, nc, nc, nbc, nbc)))
     _lib.call("esr_swe_geometry", nc, ne, nbc, _lib.ptr(_i64(mesh.src)), _lib.ptr(_i64(mesh.dst)),
               _lib.ptr(_i64(mesh.cells)), _lib.ptr(_i64(mesh.bcells)), _lib.ptr(_i64(mesh.bpoints)),
@@ -110,8 +136,33 @@ class PoissonFV:
     centroid: np.ndarray
 
 
+def _stable_csr_device(idx: torch.Tensor, n: int):
+    """rowptr [n+1], perm [m] (int32) of a device index: the stable sort
+    the reference's Reducer order follows."""
+    perm = torch.sort(idx, stable=True).indices.to(torch.int32)
+    rowptr = torch.zeros(n + 1, dtype=torch.int64, device=idx.device)
+    rowptr[1:] = torch.cumsum(torch.bincount(idx, minlength=n), 0)
+    return rowptr.to(torch.int32), perm
+
+
 def poisson_fv(mesh: TriangularMesh) -> PoissonFV:
+    """assemble_poisson.py:160-230; a mesh of CUDA tensors is assembled on
+    its device (esr_poisson_fv_assemble_device: Af, Ac, centroid bitwise the
+    host's; rho and b through CUDA's exp, within a few ulp)."""
     nc, ne, nbc = mesh.nc, mesh.ne, mesh.nbc
+    if _on_cuda(mesh):
+        dev = mesh.src.device
+        f = dict(dtype=torch.float64, device=dev)
+        out = PoissonFV(torch.empty(ne, **f), torch.empty(nc, **f), torch.empty(nc, **f), torch.empty(nc, **f),
+                        torch.empty((nc, 2), **f))
+        rowptr, perm = _stable_csr_device(mesh.src, nc)
+        brow, bperm = _stable_csr_device(mesh.bcells, nc)
+        _lib.call("esr_poisson_fv_assemble_device", nc, ne, nbc, mesh.points.shape[0], _lib.ptr(mesh.src),
+                  _lib.ptr(mesh.dst), _lib.ptr(mesh.cells), _lib.ptr(mesh.bcells), _lib.ptr(mesh.bpoints),
+                  _lib.ptr(mesh.points), _lib.ptr(rowptr), _lib.ptr(perm), _lib.ptr(brow), _lib.ptr(bperm),
+                  _lib.ptr(out.Af), _lib.ptr(out.Ac), _lib.ptr(out.b), _lib.ptr(out.rho), _lib.ptr(out.centroid),
+                  _lib.stream_handle(dev))
+        return out
     out = PoissonFV(np.empty(ne), np.empty(nc), np.empty(nc), np.empty(nc), np.empty((nc, 2)))
     _lib.call("esr_poisson_fv_assemble", nc, ne, nbc, _lib.ptr(_i64(mesh.src)), _lib.ptr(_i64(mesh.dst)),
               _lib.ptr(_i64(mesh.cells)), _lib.ptr(_i64(mesh.bcells)), _lib.ptr(_i64(mesh.bpoints)),

@@ -20,7 +20,7 @@ from .numeric import Linsys
 
 
 def _t(a, dtype=None):
-    t = torch.from_numpy(np.ascontiguousarray(a))
+    t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
     return t.to(dtype) if dtype is not None else t
 
 
@@ -88,15 +88,20 @@ class ShallowWaterEquation(esr.Module):
 def make_swe(n: int, dt: float = 5e-4, dtype: torch.dtype = torch.float64, bump: str = "centre",
              device="cpu", h=None) -> ShallowWaterEquation:
     """SWE on the n x n tutorial mesh.  bump='centre': the benchmark's
-    h = 1 + 0.1 exp(-((x-.5)^2+(y-.5)^2)/0.01); 'corner': the tutorial's."""
-    m = _mesh.triangular_mesh(n)
+    h = 1 + 0.1 exp(-((x-.5)^2+(y-.5)^2)/0.01); 'corner': the tutorial's.
+    With a CUDA ``device`` the mesh and geometry are generated on it (the
+    same values bit for bit); h is evaluated on the host either way."""
+    gen = device if torch.device(device).type == "cuda" else None
+    m = _mesh.triangular_mesh(n, device=gen)
     g = _mesh.swe_geometry(m)
     geom = dict(sx=g.sx, sy=g.sy, alpha=g.alpha, area=g.area, x=g.x, y=g.y, bsx=g.bsx, bsy=g.bsy)
     if h is None:
+        x = g.x.cpu().numpy() if isinstance(g.x, torch.Tensor) else g.x
+        y = g.y.cpu().numpy() if isinstance(g.y, torch.Tensor) else g.y
         if bump == "centre":
-            h = _mesh.gaussian_bump(g.x, g.y, 0.5, 0.5, 0.01)
+            h = _mesh.gaussian_bump(x, y, 0.5, 0.5, 0.01)
         else:
-            h = _mesh.gaussian_bump(g.x, g.y, 0.0, 0.0, 0.01)
+            h = _mesh.gaussian_bump(x, y, 0.0, 0.0, 0.01)
     eqn = ShallowWaterEquation(m.src, m.dst, m.bcells, geom, h, dt=dt, device=device)
     if dtype != torch.float64:
         eqn.to(dtype)

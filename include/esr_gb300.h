@@ -115,6 +115,44 @@ int esr_poisson_fv_assemble(int64_t nc, int64_t ne, int64_t nbc,
                             double *Af, double *Ac, double *b, double *rho,
                             double *centroid);
 
+/* esr_mesh_triangular on the GPU: every array device memory, stream-ordered
+ * on `stream`; one thread per point and per square.  Index for index and
+ * bit for bit the host generator's (csrc/triangular_mesh.cpp:10-143,
+ * get_mesh). */
+int esr_mesh_triangular_device(int64_t n, int64_t *src, int64_t *dst,
+                               int64_t *cells, int64_t *bcells,
+                               int64_t *bpoints, double *points, void *stream);
+
+/* esr_swe_geometry on the GPU (device arrays; np = number of points): one
+ * thread per cell, edge and wall face, the reference's operation order one
+ * IEEE operation at a time, so bit for bit the host's values
+ * (assemble_shallow_water.py:154-253).  An index out of range sets
+ * ESR_DEV_IDX_RANGE and leaves that entry unwritten. */
+int esr_swe_geometry_device(int64_t nc, int64_t ne, int64_t nbc, int64_t np,
+                            const int64_t *src, const int64_t *dst,
+                            const int64_t *cells, const int64_t *bcells,
+                            const int64_t *bpoints, const double *points,
+                            double *sx, double *sy, double *alpha,
+                            double *area, double *x, double *y, double *bsx,
+                            double *bsy, void *stream);
+
+/* esr_poisson_fv_assemble on the GPU (device arrays), given the stable CSR
+ * of src (rowptr [nc+1], perm [ne]) and of bcells (brow [nc+1], bperm
+ * [nbc]), int32: the in-order sums of the reference's Reducer.  Af, Ac and
+ * centroid bit for bit the host's; rho and b go through CUDA's exp (within
+ * a few ulp).  assemble_poisson.py:160-230. */
+int esr_poisson_fv_assemble_device(int64_t nc, int64_t ne, int64_t nbc,
+                                   int64_t np, const int64_t *src,
+                                   const int64_t *dst, const int64_t *cells,
+                                   const int64_t *bcells,
+                                   const int64_t *bpoints,
+                                   const double *points,
+                                   const int32_t *rowptr, const int32_t *perm,
+                                   const int32_t *brow, const int32_t *bperm,
+                                   double *Af, double *Ac, double *b,
+                                   double *rho, double *centroid,
+                                   void *stream);
+
 /* Sizes of the P1 finite-element Poisson system on an n x n square grid
  * split into 2 right triangles per square (diagonal (i,j)-(i+1,j+1)), zero
  * Dirichlet boundary: unknowns = (n-1)^2 interior nodes, nnz_off = number

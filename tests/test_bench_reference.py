@@ -11,6 +11,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 @pytest.mark.parametrize("workload,extra", [("swe", ["--n", "20"]), ("poisson", ["--n", "40"]),
+                                            ("poisson-fv", ["--n", "20"]),
                                             ("batched", ["--count", "3", "--nmin", "8", "--nmax", "12"])])
 def test_reference_arm_json_line(workload, extra):
     cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", workload,
@@ -28,6 +29,7 @@ def test_reference_arm_json_line(workload, extra):
 
 
 @pytest.mark.parametrize("workload,extra", [("swe", ["--n", "16"]), ("poisson", ["--n", "24"]),
+                                            ("poisson-fv", ["--n", "16"]),
                                             ("batched", ["--count", "3", "--nmin", "8", "--nmax", "12"])])
 def test_reference_arm_uses_no_native_code_and_our_config(workload, extra):
     """The reference arm builds its inputs with the oracle alone (this
@@ -61,5 +63,6 @@ def test_reference_arm_uses_no_native_code_and_our_config(workload, extra):
     a.dt = 5e-4 if a.n <= 1000 else 2.5e-4
     a.precision = "fast" if workload == "swe" else "native"
     a.seed = 1 if workload == "gnn" else 0
-    want = {"swe": bench.swe_config, "poisson": bench.poisson_config, "batched": bench.batched_config}[workload](a, 1)
+    want = {"swe": bench.swe_config, "poisson": bench.poisson_config, "poisson-fv": bench.poisson_config,
+            "batched": bench.batched_config}[workload](a, 1)
     assert out["line"]["config"] == want

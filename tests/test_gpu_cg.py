@@ -63,6 +63,22 @@ def test_cg_fv_n10_vs_reference(golden):
     assert info["true_residual"] <= 2e-8 * np.linalg.norm(eqn.b.collect().cpu().numpy())
 
 
+def test_cg_fv_n100_vs_reference(golden):
+    """The tutorial's FV Poisson at N=100 (40,000 cells, 119,600 edges) on
+    the fused CG, against the reference's own CG run: iterations within 2,
+    solution within 1e-7, FP64 true residual at the tolerance."""
+    g = golden("poisson_fv_n100_cg.npz")
+    eqn = workloads.make_poisson_fv(100)
+    sol = CG(eqn.A, eqn.b, eqn.x)
+    [eqn, sol] = esr.compile([eqn, sol], "cuda")
+    assert sol.fusable()
+    info = sol.solve(rtol=1e-8, maxiter=5000)
+    assert abs(info["iters"] - int(g["cg_iters"])) <= 2
+    x = eqn.x.collect().cpu().numpy()
+    assert np.linalg.norm(x - g["cg_x"]) <= 1e-7 * np.linalg.norm(g["cg_x"])
+    assert info["true_residual"] <= 1.0001e-8 * np.linalg.norm(eqn.b.collect().cpu().numpy())
+
+
 def test_cg_p1_vs_reference(golden):
     g = golden("linsys_p1_n12_cg.npz")
     eqn = _p1_module(g["row"], g["col"], g["Ae"], g["Av"], g["b"])

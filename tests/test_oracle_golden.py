@@ -88,6 +88,18 @@ def test_cg_matches_reference_fv(golden):
     assert np.linalg.norm(x.numpy() - ref) <= 1e-7 * np.linalg.norm(ref)
 
 
+def test_cg_matches_reference_fv_n100(golden):
+    """The tutorial's FV Poisson at N=100 (40,000 cells), the reference's CG
+    to relative residual 1e-8: same iterations, same solution."""
+    g = golden("poisson_fv_n100_cg.npz")
+    m = omesh.triangular_mesh(100)
+    a = omesh.poisson_fv(m)
+    x, iters, res = ocg.cg(m["src"], m["dst"], a["Af"], a["Ac"], a["b"], rtol=1e-8, maxiter=5000)
+    assert abs(iters - int(g["cg_iters"])) <= 1
+    ref = g["cg_x"]
+    assert np.linalg.norm(x.numpy() - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
 def test_cg_matches_reference_p1(golden):
     g = golden("linsys_p1_n12_cg.npz")
     x, iters, res = ocg.cg(g["row"], g["col"], g["Ae"], g["Av"], g["b"], rtol=1e-10, maxiter=1000)
