@@ -276,11 +276,17 @@ def bench_swe(args, world, rank, local):
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=dtype)
+    t_setup = time.perf_counter()
+    # mesh and geometry generated on the GPU (bitwise the host generator's)
+    eqn = workloads.make_swe(args.n, dt=args.dt, dtype=dtype, device=dev)
+    torch.cuda.synchronize(dev)
+    t_mesh = time.perf_counter() - t_setup
     if args.tile_cells:
         from easier_gb300 import swe
         swe.DEFAULT_TILE_CELLS = args.tile_cells
+    t0 = time.perf_counter()
     [eqn] = esr.compile([eqn], "cuda", precision=args.precision)
+    t_compile = time.perf_counter() - t0
     eng = eqn.easier_fused_engine
     if eng is None:
         raise RuntimeError("the fused shallow-water engine was not installed")
@@ -372,6 +378,10 @@ def bench_swe(args, world, rank, local):
                      "contract_model": "the unfused step's bytes (four delta passes and the stage combination "
                                        "through HBM): not what the fused kernel moves, so not an HBM fraction"},
         "engine": eng.describe(),
+        "setup_s": {"mesh_geometry_and_module": t_mesh,
+                    "compile": t_compile,
+                    "compile_note": "layout on the host: RCM, BFS-bisection tiles, tile/halo lists; and the "
+                                    "compile-time check of one fused step against the module's own forward"},
         "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
                    "state within 1e-5 (FP32) relative max-norm of the FP64 oracle (N=100 x 1,000 steps, N=2000 x 5 "
                    "steps)"),

@@ -627,9 +627,11 @@ int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_
 //     at fixed offsets, so a neighbour's state is three 4-byte loads from
 //     one address register.
 namespace pipe {
-constexpr int kThreads = 512;
-constexpr int kOwn = 4;                     // tile cells per thread: n0 <= 2048
-constexpr int kMaxOwn = kOwn * kThreads;
+// Two shapes of the kernel (template <int TT, int OWN, bool HREG>):
+//   512 threads x 4 tile cells (n0 <= 2048), the halo cell's records in
+//     registers too: 128 registers, 16 warps per SM;
+//   768 threads x 2 tile cells (n0 <= 1536), halo records read per stage:
+//     80 registers, 24 warps per SM.
 constexpr int kMaxLocal = 4096;             // nL
 constexpr int kBuf = 3 * kMaxLocal;         // floats of one (h, uh, vh) buffer
 constexpr int kSmemBytes = 4 * kBuf * 4;    // S0 x 2, SA, SB: 192 KB
@@ -785,15 +787,16 @@ __device__ __forceinline__ TileMeta tile_meta(const int32_t *meta, const int64_t
   return TileMeta{m[0], m[1], m[2], m[3], m[4], m[5], off3[t], offh[t]};
 }
 
-__device__ __forceinline__ bool tile_fits(const TileMeta &m, int64_t nc) {
-  return m.cell_off >= 0 && (int64_t)m.cell_off + m.n0 <= nc && m.n0 >= 0 && m.n0 <= kMaxOwn &&
+__device__ __forceinline__ bool tile_fits(const TileMeta &m, int64_t nc, int max_own) {
+  return m.cell_off >= 0 && (int64_t)m.cell_off + m.n0 <= nc && m.n0 >= 0 && m.n0 <= max_own &&
          m.nL <= kMaxLocal && m.n0 <= m.n1 && m.n1 <= m.n2 && m.n2 <= m.n3 && m.n3 <= m.nL;
 }
 
 // the own cells' state of tile m into buffer b (cp.async); the halo part
 // needs its indices first (fetch_halo)
+template <int TT>
 __device__ __forceinline__ void fetch_own(const Buf &b, const TileMeta &m, const float4 *sin) {
-  for (int j = threadIdx.x; j < m.n0; j += kThreads) fetch_state(b, j, sin, (int64_t)m.cell_off + j);
+  for (int j = threadIdx.x; j < m.n0; j += TT) fetch_state(b, j, sin, (int64_t)m.cell_off + j);
 }
 
 __device__ __forceinline__ void fetch_halo1(const Buf &b, int j, const float4 *sin, int64_t nc, int g) {
@@ -808,35 +811,40 @@ __device__ __forceinline__ void fetch_halo1(const Buf &b, int j, const float4 *s
 // the halo's state: the first two cells of this thread from the indices
 // halo_index() loaded earlier, any further ones (large halos) index and copy
 // here
+template <int TT>
 __device__ __forceinline__ void fetch_halo(const Buf &b, const TileMeta &m, const float4 *sin, int64_t nc,
                                            const int32_t *halo, const int (&hidx)[2]) {
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    const int j = m.n0 + threadIdx.x + r * kThreads;
+    const int j = m.n0 + threadIdx.x + r * TT;
     if (j < m.nL) fetch_halo1(b, j, sin, nc, hidx[r]);
   }
-  for (int j = m.n0 + threadIdx.x + 2 * kThreads; j < m.nL; j += kThreads)
+  for (int j = m.n0 + threadIdx.x + 2 * TT; j < m.nL; j += TT)
     fetch_halo1(b, j, sin, nc, __ldg(halo + m.oh + (j - m.n0)));
 }
 
+template <int TT>
 __device__ __forceinline__ void halo_index(const TileMeta &m, const int32_t *halo, int (&hidx)[2]) {
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    const int j = m.n0 + threadIdx.x + r * kThreads;
+    const int j = m.n0 + threadIdx.x + r * TT;
     hidx[r] = j < m.nL ? __ldg(halo + m.oh + (j - m.n0)) : -1;
   }
 }
 
-__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, GeoPair (&own)[kOwn / 2],
+template <int TT, int OWN, bool HREG>
+__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, GeoPair (&own)[OWN / 2],
                                               Geo &hal) {
   const float4 *slot = gslot + 3 * m.o3;
 #pragma unroll
-  for (int p = 0; p < kOwn / 2; ++p) {
-    const int jA = threadIdx.x + 2 * p * kThreads, jB = jA + kThreads;
+  for (int p = 0; p < OWN / 2; ++p) {
+    const int jA = threadIdx.x + 2 * p * TT, jB = jA + TT;
     load_pair(slot, m.n3, jA, jA < m.n0, jB, jB < m.n0, own[p]);
   }
-  const int jh = m.n0 + threadIdx.x;
-  load_geo(slot, m.n3, jh, jh < m.n3, hal);
+  if (HREG) {
+    const int jh = m.n0 + threadIdx.x;
+    load_geo(slot, m.n3, jh, jh < m.n3, hal);
+  }
 }
 
 // a halo cell (level 1..3): stage value only
@@ -852,15 +860,16 @@ __device__ __forceinline__ void halo_cell(int j, const Geo &g, int nL, const Buf
 }
 
 // one stage on the tile's own cells (pairs r, r+1) and its halo cells
-template <int STAGE>
-__device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[kOwn / 2], const Geo &hal, const Buf &in,
-                                      const Buf &s0, const Buf &out, float2 (&acc)[kOwn / 2][3], float c,
+// one stage on the tile's own cells (pairs r, r+1) and its halo cells
+template <int STAGE, int TT, int OWN, bool HREG>
+__device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[OWN / 2], const Geo &hal, const Buf &in,
+                                      const Buf &s0, const Buf &out, float2 (&acc)[OWN / 2][3], float c,
                                       float4 *sout, const float4 *gslot) {
   const float2 c2 = f2(c, c);
 #pragma unroll
-  for (int p = 0; p < kOwn / 2; ++p) {
-    const int jA = threadIdx.x + 2 * p * kThreads;
-    const int jB0 = jA + kThreads;
+  for (int p = 0; p < OWN / 2; ++p) {
+    const int jA = threadIdx.x + 2 * p * TT;
+    const int jB0 = jA + TT;
     if (jA >= m.n0) break;
     const bool vB = jB0 < m.n0;
     const int jB = vB ? jB0 : jA;
@@ -894,10 +903,14 @@ __device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[kO
   if (STAGE < 4) {  // halo cells whose level takes part in this stage
     const int lim = STAGE == 1 ? m.n3 : STAGE == 2 ? m.n2 : m.n1;
     int j = m.n0 + threadIdx.x;
-    if (j < lim) halo_cell<STAGE>(j, hal, m.nL, in, s0, out, c);
-    // more halo cells than threads (elongated tiles): face records from
-    // global memory (L1 / L2) in every stage
-    for (j += kThreads; j < lim; j += kThreads) {
+    if (HREG) {
+      if (j < lim) halo_cell<STAGE>(j, hal, m.nL, in, s0, out, c);
+      j += TT;
+    }
+    // halo cells without records in registers (all of them in the 768-thread
+    // shape; past the first TT in the other): face records from global
+    // memory (L1 / L2) in every stage
+    for (; j < lim; j += TT) {
       Geo g;
       load_geo(gslot + 3 * m.o3, m.n3, j, true, g);
       halo_cell<STAGE>(j, g, m.nL, in, s0, out, c);
@@ -907,7 +920,8 @@ __device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[kO
 
 }  // namespace pipe
 
-__global__ void __launch_bounds__(pipe::kThreads, 1)
+template <int TT, int OWN, bool HREG>
+__global__ void __launch_bounds__(TT, 1)
 swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
                      const float4 *__restrict__ gslot, const float4 *__restrict__ sin, float4 *__restrict__ sout,
@@ -918,16 +932,17 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   int t = blockIdx.x;
   if (t >= ntiles) return;
   TileMeta m = tile_meta(meta, off3, offh, t);
-  bool fits = tile_fits(m, nc);
+  constexpr int kMaxOwnT = TT * OWN;
+  bool fits = tile_fits(m, nc, kMaxOwnT);
   int cur = 0;
-  GeoPair own[kOwn / 2];
+  GeoPair own[OWN / 2];
   Geo hal;
   int hidx[2];
   if (fits) {  // prologue: the first tile's state and geometry
-    halo_index(m, halo, hidx);
-    fetch_own(Buf{smem}, m, sin);
-    fetch_halo(Buf{smem}, m, sin, nc, halo, hidx);
-    load_tile_geo(m, gslot, own, hal);
+    halo_index<TT>(m, halo, hidx);
+    fetch_own<TT>(Buf{smem}, m, sin);
+    fetch_halo<TT>(Buf{smem}, m, sin, nc, halo, hidx);
+    load_tile_geo<TT, OWN, HREG>(m, gslot, own, hal);
   }
   cp_commit();
   while (true) {
@@ -936,41 +951,41 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
     bool next = tn < ntiles;
     if (next) {
       mn = tile_meta(meta, off3, offh, tn);
-      if (!tile_fits(mn, nc)) {  // outside the kernel's limits: flag it, leave its cells unwritten
+      if (!tile_fits(mn, nc, kMaxOwnT)) {  // outside the kernel's limits: flag it, leave its cells unwritten
         esr::raise_status(ESR_DEV_IDX_RANGE);
       }
     }
     cp_wait_all();
     __syncthreads();  // this tile's state is in buffer `cur`; the other buffer is free
     const Buf S0{smem + cur * kBuf}, S0n{smem + (cur ^ 1) * kBuf};
-    const bool nfit = next && tile_fits(mn, nc);
+    const bool nfit = next && tile_fits(mn, nc, kMaxOwnT);
     if (nfit) {
       if (threadIdx.x == 0) {  // the next tile's face records into L2
         const float4 *g = gslot + 3 * mn.o3;
         const unsigned bytes = (unsigned)(3 * (int64_t)mn.n3 * 16);
         if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g), "r"(bytes) : "memory");
       }
-      halo_index(mn, halo, hidx);
-      fetch_own(S0n, mn, sin);
+      halo_index<TT>(mn, halo, hidx);
+      fetch_own<TT>(S0n, mn, sin);
     }
     if (fits) {
-      float2 acc[kOwn / 2][3];
-      stage<1>(m, own, hal, S0, S0, SA, acc, c1, sout, gslot);
-      if (nfit) fetch_halo(S0n, mn, sin, nc, halo, hidx);
+      float2 acc[OWN / 2][3];
+      stage<1, TT, OWN, HREG>(m, own, hal, S0, S0, SA, acc, c1, sout, gslot);
+      if (nfit) fetch_halo<TT>(S0n, mn, sin, nc, halo, hidx);
       cp_commit();
       __syncthreads();
-      stage<2>(m, own, hal, SA, S0, SB, acc, c1, sout, gslot);
+      stage<2, TT, OWN, HREG>(m, own, hal, SA, S0, SB, acc, c1, sout, gslot);
       __syncthreads();
-      stage<3>(m, own, hal, SB, S0, SA, acc, c3, sout, gslot);
+      stage<3, TT, OWN, HREG>(m, own, hal, SB, S0, SA, acc, c3, sout, gslot);
       __syncthreads();
-      stage<4>(m, own, hal, SA, S0, SA, acc, c4, sout, gslot);
+      stage<4, TT, OWN, HREG>(m, own, hal, SA, S0, SA, acc, c4, sout, gslot);
     } else {
-      if (nfit) fetch_halo(S0n, mn, sin, nc, halo, hidx);
+      if (nfit) fetch_halo<TT>(S0n, mn, sin, nc, halo, hidx);
       cp_commit();
     }
     if (!next) break;
     // the next tile's geometry: this thread is done with the current one
-    if (nfit) load_tile_geo(mn, gslot, own, hal);
+    if (nfit) load_tile_geo<TT, OWN, HREG>(mn, gslot, own, hal);
     m = mn;
     fits = nfit;
     t = tn;
@@ -979,13 +994,23 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   cp_wait_all();
 }
 
-bool pipe_fits(const esr_swe_tiles *T) {
-  return !T->exact && T->max_own <= pipe::kMaxOwn && T->max_local <= pipe::kMaxLocal;
+// CTA shapes of the pipelined kernel: 512 threads x 4 tile cells (what
+// PIPELINED and AUTO run; measured fastest at N=2000 with 1,900-cell tiles)
+// and 768 threads x 2 (n0 <= 1536; on request)
+constexpr int kPipeSmall = 768 * 2, kPipeLarge = 512 * 4;
+
+bool pipe_fits(const esr_swe_tiles *T, int shape) {
+  const int max_own = shape == ESR_SWE_TILE_PIPELINED_768 ? kPipeSmall : kPipeLarge;
+  return !T->exact && T->max_own <= max_own && T->max_local <= pipe::kMaxLocal;
 }
 
-int run_pipe(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       pipe::kSmemBytes);
+int pipe_shape(const esr_swe_tiles *) { return ESR_SWE_TILE_PIPELINED_512; }
+
+template <int TT, int OWN, bool HREG>
+int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
+                   cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel<TT, OWN, HREG>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::kSmemBytes);
   if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/pipelined smem attribute");
   int dev = 0, sms = 0;
   e = cudaGetDevice(&dev);
@@ -995,12 +1020,19 @@ int run_pipe(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b
   const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
   float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
   for (int64_t k = 0; k < steps; ++k) {
-    swe_tile_pipe_kernel<<<grid, pipe::kThreads, pipe::kSmemBytes, s>>>(
+    swe_tile_pipe_kernel<TT, OWN, HREG><<<grid, TT, pipe::kSmemBytes, s>>>(
         tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots, buf[k & 1],
         buf[(k + 1) & 1], tiles->nc, tiles->ntiles, c1, c3, c4);
   }
   ESR_LAUNCH_CHECK("esr_swe_tile_step/pipelined");
   return ESR_OK;
+}
+
+int run_pipe(const esr_swe_tiles *tiles, int shape, double dt, void *state_a, void *state_b, int64_t steps,
+             cudaStream_t s) {
+  if (shape == ESR_SWE_TILE_PIPELINED_768)
+    return run_pipe_shape<768, 2, false>(tiles, dt, state_a, state_b, steps, s);
+  return run_pipe_shape<512, 4, true>(tiles, dt, state_a, state_b, steps, s);
 }
 
 }  // namespace
@@ -1054,7 +1086,7 @@ extern "C" int esr_swe_tile_threads(const esr_swe_tiles *tiles) {
 
 extern "C" int esr_swe_tile_kernel(const esr_swe_tiles *tiles) {
   if (check_tiles(tiles)) return -1;
-  return pipe_fits(tiles) ? ESR_SWE_TILE_PIPELINED : ESR_SWE_TILE_BLOCKED;
+  return pipe_fits(tiles, ESR_SWE_TILE_PIPELINED_512) ? pipe_shape(tiles) : ESR_SWE_TILE_BLOCKED;
 }
 
 extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, double dt, void *state_a,
@@ -1064,15 +1096,18 @@ extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, do
   if (steps < 0) return esr::fail(ESR_ERR_ARG, "negative step count");
   if (!state_a || !state_b || state_a == state_b) return esr::fail(ESR_ERR_ARG, "need two distinct state buffers");
   if (((uintptr_t)state_a | (uintptr_t)state_b) % 16) return esr::fail(ESR_ERR_ARG, "state buffers must be 16-byte aligned");
-  if (kernel == ESR_SWE_TILE_AUTO) kernel = pipe_fits(tiles) ? ESR_SWE_TILE_PIPELINED : ESR_SWE_TILE_BLOCKED;
-  if (kernel == ESR_SWE_TILE_PIPELINED && !pipe_fits(tiles))
-    return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, <= 2048 own cells and "
-                                          "<= 4096 local cells a tile");
-  if (kernel != ESR_SWE_TILE_PIPELINED && kernel != ESR_SWE_TILE_BLOCKED)
+  if (kernel == ESR_SWE_TILE_AUTO) kernel = esr_swe_tile_kernel(tiles);
+  if (kernel == ESR_SWE_TILE_PIPELINED) kernel = pipe_shape(tiles);
+  if (kernel == ESR_SWE_TILE_PIPELINED_512 || kernel == ESR_SWE_TILE_PIPELINED_768) {
+    if (!pipe_fits(tiles, kernel))
+      return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, <= 4096 local cells a "
+                                            "tile and <= 2048 own cells (512-thread shape) or <= 1536 (768-thread)");
+  } else if (kernel != ESR_SWE_TILE_BLOCKED) {
     return esr::fail(ESR_ERR_ARG, "unknown tile kernel");
+  }
   if (steps == 0) return ESR_OK;
   cudaStream_t s = esr::as_stream(stream);
-  if (kernel == ESR_SWE_TILE_PIPELINED) return run_pipe(tiles, dt, state_a, state_b, steps, s);
+  if (kernel != ESR_SWE_TILE_BLOCKED) return run_pipe(tiles, kernel, dt, state_a, state_b, steps, s);
   return tiles->exact ? run_tiles<true>(tiles, dt, state_a, state_b, steps, s)
                       : run_tiles<false>(tiles, dt, state_a, state_b, steps, s);
 }

@@ -349,19 +349,25 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
  *   BLOCKED: one CTA per tile (1024, 512 or 256 threads), the face records
  *     read from global memory in every stage; any layout within the limits
  *     above, exact or fast arithmetic;
- *   PIPELINED: fast arithmetic only; one persistent 512-thread CTA per SM,
- *     each thread's face records (4 tile cells, 1 halo cell) held in
- *     registers through the four stages, the next tile's state copied into
- *     shared memory (cp.async) and its records prefetched into L2 while the
- *     current tile computes, two cells per thread in packed FP32x2
- *     arithmetic.  Needs n0 <= 2048 and nL <= 4096 in every tile.
- * AUTO picks PIPELINED when the layout allows it. */
+ *   PIPELINED: fast arithmetic only; one persistent CTA per SM, each
+ *     thread's tile-cell face records held in registers through the four
+ *     stages, the next tile's state copied into shared memory (cp.async)
+ *     and its records prefetched into L2 while the current tile computes,
+ *     two cells per thread in packed FP32x2 arithmetic.  Two CTA shapes:
+ *     PIPELINED_512 (512 threads x 4 tile cells, n0 <= 2048, the halo
+ *     cell's records in registers too) and PIPELINED_768 (768 threads x 2,
+ *     n0 <= 1536, the halo's records read per stage); PIPELINED is the
+ *     512-thread shape.  Needs nL <= 4096 in every tile.
+ * AUTO picks a pipelined shape when the layout allows it. */
 #define ESR_SWE_TILE_AUTO 0
 #define ESR_SWE_TILE_BLOCKED 1
 #define ESR_SWE_TILE_PIPELINED 2
+#define ESR_SWE_TILE_PIPELINED_512 3
+#define ESR_SWE_TILE_PIPELINED_768 4
 
-/* The kernel AUTO runs for this layout, or -1 if the layout is outside the
- * limits.  No reference counterpart. */
+/* The kernel AUTO runs for this layout (BLOCKED, PIPELINED_512 or
+ * PIPELINED_768), or -1 if the layout is outside the limits.  No reference
+ * counterpart. */
 int esr_swe_tile_kernel(const esr_swe_tiles *tiles);
 
 /* esr_swe_tile_step on a chosen kernel (ESR_ERR_UNSUPPORTED if the layout

@@ -206,7 +206,7 @@ def test_full_size_tiled_equals_staged_and_conserves_mass(monkeypatch):
         assert torch.equal(a, b)
 
 
-@pytest.mark.parametrize("n,target", [(37, None), (150, 300), (300, None), (400, 700)])
+@pytest.mark.parametrize("n,target", [(37, None), (150, 300), (300, None), (400, 700), (400, 1450)])
 def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypatch):
     """Fast arithmetic: the persistent pipelined tile kernel (state of the
     next tile prefetched, geometry in registers, packed FP32x2 arithmetic)
@@ -219,10 +219,13 @@ def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypa
     eqn = workloads.make_swe(n, dt=5e-4, dtype=torch.float32)
     [eqn] = esr.compile([eqn], "cuda", precision="fast")
     eng = eqn.easier_fused_engine
-    assert eng.tiled and eng.tile_kernel_name() == "pipelined", eng.describe()
+    assert eng.tiled and eng.tile_kernel_name().startswith("pipelined"), eng.describe()
     s0 = eng.state.clone()
     outs = []
-    for kern in ("pipelined", "blocked"):
+    kernels = ["pipelined_512", "blocked"]
+    if eng.tile_stats["max_own"] <= 1536:
+        kernels.append("pipelined_768")
+    for kern in kernels:
         eng.tile_kernel = kern
         eng.state.copy_(s0)
         eng.step(7)
@@ -230,4 +233,5 @@ def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypa
         outs.append(eng.state.clone())
     from easier_gb300 import ops
     assert ops.device_status() == 0
-    assert torch.equal(outs[0], outs[1])
+    for o in outs[1:]:
+        assert torch.equal(outs[0], o)
