@@ -557,7 +557,12 @@ def bench_batched(args, world, rank, local):
     eng = BatchedPCG(insts, jacobi=True, precision=prec, device=dev, graph_iters=args.chunk)
     prep = time.perf_counter() - t0
     t0 = time.perf_counter()
-    tuning = eng.autotune() if not args.no_autotune else None
+    if args.shape:  # a fixed work shape (tiles per chunk, CTAs), e.g. the one autotune picks
+        tpc, grid = (int(v) for v in args.shape.split(","))
+        eng.set_shape(tpc, grid)
+        tuning = None
+    else:
+        tuning = eng.autotune() if not args.no_autotune else None
     tune_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream(dev)
     x_start = torch.zeros_like(eng.b64)
@@ -828,6 +833,7 @@ def bench_reference(args, world):
         unit, metric = "cell-steps/s", "SWE cell-steps/s"
         sample = f"{args.steps} full oracle steps at N={args.n} ({nc} cells), {args.dtype}"
         cfg = swe_config(args, world)
+        eager = _swe_eager_gpu(m, g, h, args, dtype) if torch.cuda.is_available() else None
     elif args.workload in ("batched", "gnn"):
         from easier_gb300 import mesh as gen  # numpy generators of the seeded fields and right hand sides
         from easier_gb300.numeric.batched import p1_sides
@@ -891,12 +897,43 @@ def bench_reference(args, world):
     if args.steps < requested:
         sample += f"; {args.steps} of the {requested} requested steps fit the {REF_BUDGET_S:.0f} s budget"
     sample += f"; oracle input set-up {setup:.1f} s (not timed)"
-    return {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype if args.workload == "swe" else "f64",
             "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.workload == "swe" and eager is not None:
+        line["reference_eager_gpu"] = eager
+    return line
+
+
+def _swe_eager_gpu(m, g, h, args, dtype, steps=10):
+    """The second baseline: the reference's SWE op sequence (aten index
+    gathers, scatter_reduce_ with atomics, elementwise ops) as eager torch
+    kernels on this GPU -- what its backend='cuda' runs, without its
+    JitEngine interpreter -- timed with CUDA events."""
+    from oracle import swe as oswe
+    dev = torch.device("cuda", 0)
+    p = oswe.SweProblem(m["src"], m["dst"], m["bcells"], g["sx"], g["sy"], g["alpha"], g["bsx"], g["bsy"],
+                        g["area"], args.dt, dtype, device=dev)
+    st = [h.to(dev), torch.zeros_like(h, device=dev), torch.zeros_like(h, device=dev)]
+    st[:] = p.step(*st)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        st[:] = p.step(*st)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    nc = int(h.shape[0])
+    out = {"value": nc / (ms / 1e3), "unit": "cell-steps/s", "ms_per_step": ms, "steps": steps,
+           "path": "reference op sequence as eager torch on the GPU (aten index + scatter_reduce_ with atomics; "
+                   "the reference's backend='cuda' without its interpreter)"}
+    del p, st
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -913,6 +950,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=32, help="batched: iterations per CUDA graph")
     ap.add_argument("--no-autotune", action="store_true", help="batched: keep the default work shape")
     ap.add_argument("--polled", action="store_true", help="batched: host-polled graphs instead of one launch")
+    ap.add_argument("--shape", default=None, help="batched: fixed work shape TILES_PER_CHUNK,CTAS (no autotune)")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
     ap.add_argument("--dt", type=float, default=None)

@@ -60,6 +60,10 @@ DEFAULT_TILE_CELLS: Optional[int] = None
 TILE_MAX_L3 = 6144      # kernel limit on tile + 3 halo rings
 TILE_SMEM = 227 * 1024  # shared memory per CTA
 DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
+# Numbering before the tile partition of a tiled layout: "rcm" (reverse
+# Cuthill-McKee, then tile-major) or "tiles" (the module's own order, then
+# tile-major: the partition alone, without the RCM pass)
+TILED_REORDER = "rcm"
 # Fast arithmetic on large meshes: tiles for the pipelined tile kernel
 # (<= 2048 own cells, <= 4096 local cells)
 PIPE_TILE_TARGET = 1900
@@ -153,7 +157,8 @@ class SweEngine:
         tile_cells = self.tile_cells
         pipe_tries = 0
         while True:
-            lay = cell_layout(nc, src, dst, bcell, reorder=self.reorder,
+            reorder = TILED_REORDER if (want_tiles and self.reorder == "rcm") else self.reorder
+            lay = cell_layout(nc, src, dst, bcell, reorder=reorder,
                               tile_cells=tile_cells if want_tiles else None)
             if lay["part"] is None:
                 break

@@ -9,11 +9,14 @@ import torch
 
 
 class SweProblem:
-    def __init__(self, src, dst, bcells, sx, sy, alpha, bsx, bsy, area, dt, dtype=torch.float64):
-        t = lambda a: torch.as_tensor(a).to(dtype)  # noqa: E731
-        self.src = torch.as_tensor(src, dtype=torch.int64)
-        self.dst = torch.as_tensor(dst, dtype=torch.int64)
-        self.bcells = torch.as_tensor(bcells, dtype=torch.int64)
+    def __init__(self, src, dst, bcells, sx, sy, alpha, bsx, bsy, area, dt, dtype=torch.float64, device="cpu"):
+        """device: where the aten ops run (a CUDA device runs the reference's
+        op sequence as eager CUDA kernels: its backend='cuda' path without
+        the JitEngine interpreter)."""
+        t = lambda a: torch.as_tensor(a).to(device=device, dtype=dtype)  # noqa: E731
+        self.src = torch.as_tensor(src, dtype=torch.int64).to(device)
+        self.dst = torch.as_tensor(dst, dtype=torch.int64).to(device)
+        self.bcells = torch.as_tensor(bcells, dtype=torch.int64).to(device)
         self.sx, self.sy, self.alpha = t(sx), t(sy), t(alpha)
         self.bsx, self.bsy, self.area = t(bsx), t(bsy), t(area)
         self.nc = self.area.shape[0]
@@ -21,7 +24,8 @@ class SweProblem:
         self.dtype = dtype
 
     def _scatter(self, idx, v):
-        return torch.zeros(self.nc, dtype=v.dtype).scatter_reduce_(0, idx, v, "sum", include_self=False)
+        return torch.zeros(self.nc, dtype=v.dtype, device=v.device).scatter_reduce_(0, idx, v, "sum",
+                                                                                 include_self=False)
 
     def face_reconstruct(self, phi):
         return (1 - self.alpha) * phi[self.src] + self.alpha * phi[self.dst]
@@ -56,7 +60,7 @@ class SweProblem:
         return h, uh, vh
 
     def run(self, h, uh, vh, steps):
-        h, uh, vh = (torch.as_tensor(a).to(self.dtype).clone() for a in (h, uh, vh))
+        h, uh, vh = (torch.as_tensor(a).to(device=self.src.device, dtype=self.dtype).clone() for a in (h, uh, vh))
         for _ in range(steps):
             h, uh, vh = self.step(h, uh, vh)
         return h, uh, vh
