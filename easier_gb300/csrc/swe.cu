@@ -613,25 +613,25 @@ int run_tiles(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_
 // Same tiles, same arithmetic and order as swe_tile_step_kernel<fast>, so
 // the result is bitwise the same; organised for GB300's latency and issue
 // limits instead of one CTA per tile:
-//   * persistent: one 512-thread CTA per SM walks tiles t, t + grid, ...;
-//   * the face geometry of the cells a thread owns (4 tile cells and 1 halo
-//     cell of level 1..3) is loaded into registers once per step and kept
-//     through the four stages (the stages touch shared memory only);
+//   * persistent: one CTA per SM walks tiles t, t + grid, ...;
+//   * thread x of a TT-thread CTA computes the local cells j = x + r*TT,
+//     r < CELLS, whatever their level (tile cells first, then the halo of
+//     levels 1..3), as CELLS/2 pairs: every thread has the same number of
+//     cells in a stage, so no warp waits at the stage barriers for another
+//     one's extra halo cell;
+//   * the face records of those cells are loaded into registers once per
+//     step and kept through the four stages (the stages touch shared memory
+//     only); local cells past CELLS*TT (large halos) read theirs per stage;
 //   * the next tile's state (own cells and halo) is copied into a second
 //     shared-memory buffer with cp.async while this tile computes, and its
 //     face records are prefetched into L2 with one bulk prefetch;
-//   * two tile cells are computed in lock step with the packed FP32x2
-//     instructions (__ffma2_rn, __fadd2_rn, __fmul2_rn: per lane the
+//   * the two cells of a pair are computed in lock step with the packed
+//     FP32x2 instructions (__ffma2_rn, __fadd2_rn, __fmul2_rn: per lane the
 //     IEEE operations of the scalar kernel), halving the FP instructions;
 //   * stage states live in shared memory as three float arrays (h, uh, vh)
 //     at fixed offsets, so a neighbour's state is three 4-byte loads from
 //     one address register.
 namespace pipe {
-// Two shapes of the kernel (template <int TT, int OWN, bool HREG>):
-//   512 threads x 4 tile cells (n0 <= 2048), the halo cell's records in
-//     registers too: 128 registers, 16 warps per SM;
-//   768 threads x 2 tile cells (n0 <= 1536), halo records read per stage:
-//     80 registers, 24 warps per SM.
 constexpr int kMaxLocal = 4096;             // nL
 constexpr int kBuf = 3 * kMaxLocal;         // floats of one (h, uh, vh) buffer
 constexpr int kSmemBytes = 4 * kBuf * 4;    // S0 x 2, SA, SB: 192 KB
@@ -706,9 +706,8 @@ __device__ __forceinline__ void face1(float &Sh, float &Su, float &Sv, float oh,
   }
 }
 
-// Face records of two tile cells A, B, held as the lanes of float2 values
-// so the packed arithmetic takes them without re-pairing registers in
-// every stage.
+// Face records of two cells A, B, held as the lanes of float2 values so the
+// packed arithmetic takes them without re-pairing registers in every stage.
 struct GeoPair {
   float2 sx[3], sy[3], al[3];
   int nbA[3], nbB[3];
@@ -832,50 +831,52 @@ __device__ __forceinline__ void halo_index(const TileMeta &m, const int32_t *hal
   }
 }
 
-template <int TT, int OWN, bool HREG>
-__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, GeoPair (&own)[OWN / 2],
-                                              Geo &hal) {
+// records of the local cells x + r*TT, r < CELLS, of level <= 3
+template <int TT, int CELLS>
+__device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *gslot, GeoPair (&gp)[CELLS / 2]) {
   const float4 *slot = gslot + 3 * m.o3;
 #pragma unroll
-  for (int p = 0; p < OWN / 2; ++p) {
+  for (int p = 0; p < CELLS / 2; ++p) {
     const int jA = threadIdx.x + 2 * p * TT, jB = jA + TT;
-    load_pair(slot, m.n3, jA, jA < m.n0, jB, jB < m.n0, own[p]);
-  }
-  if (HREG) {
-    const int jh = m.n0 + threadIdx.x;
-    load_geo(slot, m.n3, jh, jh < m.n3, hal);
+    load_pair(slot, m.n3, jA, jA < m.n3, jB, jB < m.n3, gp[p]);
   }
 }
 
-// a halo cell (level 1..3): stage value only
+// a local cell past CELLS*TT (a large halo): its records from global memory
+// (L1 / L2), scalar
 template <int STAGE>
-__device__ __forceinline__ void halo_cell(int j, const Geo &g, int nL, const Buf &in, const Buf &s0, const Buf &out,
-                                          float c) {
+__device__ __forceinline__ void extra_cell(int j, const TileMeta &m, const float4 *gslot, const Buf &in,
+                                           const Buf &s0, const Buf &out, float c) {
+  Geo g;
+  load_geo(gslot + 3 * m.o3, m.n3, j, true, g);
   const float oh = in.h(j), ou = in.u(j), ov = in.v(j);
   float Sh = 0.f, Su = 0.f, Sv = 0.f;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) face1(Sh, Su, Sv, oh, ou, ov, in, g.nb[k], nL, g.al[k], g.sx[k], g.sy[k]);
+  for (int k = 0; k < 3; ++k) face1(Sh, Su, Sv, oh, ou, ov, in, g.nb[k], m.nL, g.al[k], g.sx[k], g.sy[k]);
   const float h0 = STAGE == 1 ? oh : s0.h(j), u0 = STAGE == 1 ? ou : s0.u(j), v0 = STAGE == 1 ? ov : s0.v(j);
   out.put(j, fmaf(c, -Sh, h0), fmaf(c, -Su, u0), fmaf(c, -Sv, v0));
 }
 
-// one stage on the tile's own cells (pairs r, r+1) and its halo cells
-// one stage on the tile's own cells (pairs r, r+1) and its halo cells
-template <int STAGE, int TT, int OWN, bool HREG>
-__device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[OWN / 2], const Geo &hal, const Buf &in,
-                                      const Buf &s0, const Buf &out, float2 (&acc)[OWN / 2][3], float c,
+// One stage: cells j < lim (n3, n2, n1 for stages 1-3; the tile, j < n0,
+// for stage 4).  Tile cells add their delta to `acc` (stages 1-3) and
+// combine it into the new state (stage 4); halo cells only give their stage
+// value.  acc lanes of halo cells hold values nobody reads.
+template <int STAGE, int TT, int CELLS>
+__device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&gp)[CELLS / 2], const Buf &in,
+                                      const Buf &s0, const Buf &out, float2 (&acc)[CELLS / 2][3], float c,
                                       float4 *sout, const float4 *gslot) {
   const float2 c2 = f2(c, c);
+  const int lim = STAGE == 1 ? m.n3 : STAGE == 2 ? m.n2 : STAGE == 3 ? m.n1 : m.n0;
 #pragma unroll
-  for (int p = 0; p < OWN / 2; ++p) {
+  for (int p = 0; p < CELLS / 2; ++p) {
     const int jA = threadIdx.x + 2 * p * TT;
     const int jB0 = jA + TT;
-    if (jA >= m.n0) break;
-    const bool vB = jB0 < m.n0;
+    if (jA >= lim) break;
+    const bool vB = jB0 < lim;
     const int jB = vB ? jB0 : jA;
     const float2 oh = f2(in.h(jA), in.h(jB)), ou = f2(in.u(jA), in.u(jB)), ov = f2(in.v(jA), in.v(jB));
     float2 dh, du, dv;
-    delta2(own[p], oh, ou, ov, in, m.nL, dh, du, dv);
+    delta2(gp[p], oh, ou, ov, in, m.nL, dh, du, dv);
     const float2 h0 = STAGE == 1 ? oh : f2(s0.h(jA), s0.h(jB));
     const float2 u0 = STAGE == 1 ? ou : f2(s0.u(jA), s0.u(jB));
     const float2 v0 = STAGE == 1 ? ov : f2(s0.v(jA), s0.v(jB));
@@ -900,27 +901,13 @@ __device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&own)[OW
       if (vB) sout[(int64_t)m.cell_off + jB] = make_float4(xh.y, xu.y, xv.y, 0.f);
     }
   }
-  if (STAGE < 4) {  // halo cells whose level takes part in this stage
-    const int lim = STAGE == 1 ? m.n3 : STAGE == 2 ? m.n2 : m.n1;
-    int j = m.n0 + threadIdx.x;
-    if (HREG) {
-      if (j < lim) halo_cell<STAGE>(j, hal, m.nL, in, s0, out, c);
-      j += TT;
-    }
-    // halo cells without records in registers (all of them in the 768-thread
-    // shape; past the first TT in the other): face records from global
-    // memory (L1 / L2) in every stage
-    for (; j < lim; j += TT) {
-      Geo g;
-      load_geo(gslot + 3 * m.o3, m.n3, j, true, g);
-      halo_cell<STAGE>(j, g, m.nL, in, s0, out, c);
-    }
-  }
+  if (STAGE < 4)  // local cells beyond the register-held ones (the tile's fit in them)
+    for (int j = threadIdx.x + CELLS * TT; j < lim; j += TT) extra_cell<STAGE>(j, m, gslot, in, s0, out, c);
 }
 
 }  // namespace pipe
 
-template <int TT, int OWN, bool HREG>
+template <int TT, int CELLS>
 __global__ void __launch_bounds__(TT, 1)
 swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
@@ -932,17 +919,18 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
   int t = blockIdx.x;
   if (t >= ntiles) return;
   TileMeta m = tile_meta(meta, off3, offh, t);
-  constexpr int kMaxOwnT = TT * OWN;
+  constexpr int kMaxOwnT = TT * CELLS;  // the tile's cells are among the register-held ones
   bool fits = tile_fits(m, nc, kMaxOwnT);
   int cur = 0;
-  GeoPair own[OWN / 2];
-  Geo hal;
+  GeoPair gp[CELLS / 2];
   int hidx[2];
   if (fits) {  // prologue: the first tile's state and geometry
     halo_index<TT>(m, halo, hidx);
     fetch_own<TT>(Buf{smem}, m, sin);
     fetch_halo<TT>(Buf{smem}, m, sin, nc, halo, hidx);
-    load_tile_geo<TT, OWN, HREG>(m, gslot, own, hal);
+    load_tile_geo<TT, CELLS>(m, gslot, gp);
+  } else {
+    esr::raise_status(ESR_DEV_IDX_RANGE);
   }
   cp_commit();
   while (true) {
@@ -969,23 +957,23 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
       fetch_own<TT>(S0n, mn, sin);
     }
     if (fits) {
-      float2 acc[OWN / 2][3];
-      stage<1, TT, OWN, HREG>(m, own, hal, S0, S0, SA, acc, c1, sout, gslot);
+      float2 acc[CELLS / 2][3];
+      stage<1, TT, CELLS>(m, gp, S0, S0, SA, acc, c1, sout, gslot);
       if (nfit) fetch_halo<TT>(S0n, mn, sin, nc, halo, hidx);
       cp_commit();
       __syncthreads();
-      stage<2, TT, OWN, HREG>(m, own, hal, SA, S0, SB, acc, c1, sout, gslot);
+      stage<2, TT, CELLS>(m, gp, SA, S0, SB, acc, c1, sout, gslot);
       __syncthreads();
-      stage<3, TT, OWN, HREG>(m, own, hal, SB, S0, SA, acc, c3, sout, gslot);
+      stage<3, TT, CELLS>(m, gp, SB, S0, SA, acc, c3, sout, gslot);
       __syncthreads();
-      stage<4, TT, OWN, HREG>(m, own, hal, SA, S0, SA, acc, c4, sout, gslot);
+      stage<4, TT, CELLS>(m, gp, SA, S0, SA, acc, c4, sout, gslot);
     } else {
       if (nfit) fetch_halo<TT>(S0n, mn, sin, nc, halo, hidx);
       cp_commit();
     }
     if (!next) break;
     // the next tile's geometry: this thread is done with the current one
-    if (nfit) load_tile_geo<TT, OWN, HREG>(mn, gslot, own, hal);
+    if (nfit) load_tile_geo<TT, CELLS>(mn, gslot, gp);
     m = mn;
     fits = nfit;
     t = tn;
@@ -1006,10 +994,10 @@ bool pipe_fits(const esr_swe_tiles *T, int shape) {
 
 int pipe_shape(const esr_swe_tiles *) { return ESR_SWE_TILE_PIPELINED_512; }
 
-template <int TT, int OWN, bool HREG>
+template <int TT, int CELLS>
 int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
                    cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel<TT, OWN, HREG>,
+  cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel<TT, CELLS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::kSmemBytes);
   if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/pipelined smem attribute");
   int dev = 0, sms = 0;
@@ -1020,7 +1008,7 @@ int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *s
   const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
   float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
   for (int64_t k = 0; k < steps; ++k) {
-    swe_tile_pipe_kernel<TT, OWN, HREG><<<grid, TT, pipe::kSmemBytes, s>>>(
+    swe_tile_pipe_kernel<TT, CELLS><<<grid, TT, pipe::kSmemBytes, s>>>(
         tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots, buf[k & 1],
         buf[(k + 1) & 1], tiles->nc, tiles->ntiles, c1, c3, c4);
   }
@@ -1031,8 +1019,8 @@ int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *s
 int run_pipe(const esr_swe_tiles *tiles, int shape, double dt, void *state_a, void *state_b, int64_t steps,
              cudaStream_t s) {
   if (shape == ESR_SWE_TILE_PIPELINED_768)
-    return run_pipe_shape<768, 2, false>(tiles, dt, state_a, state_b, steps, s);
-  return run_pipe_shape<512, 4, true>(tiles, dt, state_a, state_b, steps, s);
+    return run_pipe_shape<768, 2>(tiles, dt, state_a, state_b, steps, s);
+  return run_pipe_shape<512, 4>(tiles, dt, state_a, state_b, steps, s);
 }
 
 }  // namespace

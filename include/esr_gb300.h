@@ -353,11 +353,12 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
  *     thread's tile-cell face records held in registers through the four
  *     stages, the next tile's state copied into shared memory (cp.async)
  *     and its records prefetched into L2 while the current tile computes,
- *     two cells per thread in packed FP32x2 arithmetic.  Two CTA shapes:
- *     PIPELINED_512 (512 threads x 4 tile cells, n0 <= 2048, the halo
- *     cell's records in registers too) and PIPELINED_768 (768 threads x 2,
- *     n0 <= 1536, the halo's records read per stage); PIPELINED is the
- *     512-thread shape.  Needs nL <= 4096 in every tile.
+ *     cells (tile and halo alike) assigned round-robin and computed in
+ *     pairs with packed FP32x2 arithmetic.  Two CTA shapes, by the cells a
+ *     thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
+ *     n0 <= 2048) and PIPELINED_768 (768 threads x 2, n0 <= 1536); cells
+ *     of level <= 3 past those read their records per stage.  PIPELINED is
+ *     the 512-thread shape.  Needs nL <= 4096 in every tile.
  * AUTO picks a pipelined shape when the layout allows it. */
 #define ESR_SWE_TILE_AUTO 0
 #define ESR_SWE_TILE_BLOCKED 1

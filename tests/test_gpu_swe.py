@@ -206,7 +206,7 @@ def test_full_size_tiled_equals_staged_and_conserves_mass(monkeypatch):
         assert torch.equal(a, b)
 
 
-@pytest.mark.parametrize("n,target", [(37, None), (150, 300), (300, None), (400, 700), (400, 1450)])
+@pytest.mark.parametrize("n,target", [(37, None), (150, 300), (300, None), (400, 700), (400, 1450), (400, 1900)])
 def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypatch):
     """Fast arithmetic: the persistent pipelined tile kernel (state of the
     next tile prefetched, geometry in registers, packed FP32x2 arithmetic)
