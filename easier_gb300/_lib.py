@@ -32,10 +32,10 @@ class SweMesh(Structure):
 
 class SweTiles(Structure):
     _fields_ = [("nc", c_int64), ("ntiles", c_int32), ("dtype", c_int32), ("max_local", c_int32),
-                ("max_l3", c_int32), ("max_own", c_int32), ("pad_", c_int32),
+                ("max_l3", c_int32), ("max_own", c_int32), ("max_halo3", c_int32),
                 ("meta", c_void_p), ("off3", c_void_p), ("offh", c_void_p), ("halo", c_void_p),
                 ("slots", c_void_p), ("area", c_void_p), ("inv_area", c_void_p), ("exact", c_int32),
-                ("pad2_", c_int32)]
+                ("slot_info", c_int32)]
 
 
 SWE_TILE_AUTO, SWE_TILE_BLOCKED, SWE_TILE_PIPELINED = 0, 1, 2

@@ -713,10 +713,28 @@ struct GeoPair {
   int nbA[3], nbB[3];
 };
 
-__device__ __forceinline__ void load_pair(const float4 *slot, int n3, int jA, bool vA, int jB, bool vB, GeoPair &g) {
+// Slots 1 and 2 of a cell are interior faces (the layout's slot_info
+// promise; walls and empty slots sort into slot 0): a cell past the tile's
+// end gets faces there that contribute nothing (neighbour 0, zero normal),
+// and a slot that breaks the promise is flagged and gets the same.
+__device__ __forceinline__ void interior_slots(Geo &g, int nL, bool valid) {
+#pragma unroll
+  for (int k = 1; k < 3; ++k) {
+    if ((unsigned)g.nb[k] >= (unsigned)nL) {
+      if (valid) esr::raise_status(ESR_DEV_IDX_RANGE);
+      g.nb[k] = 0;
+      g.sx[k] = g.sy[k] = g.al[k] = 0.f;
+    }
+  }
+}
+
+__device__ __forceinline__ void load_pair(const float4 *slot, int n3, int nL, int jA, bool vA, int jB, bool vB,
+                                          GeoPair &g) {
   Geo a, b;
   load_geo(slot, n3, jA, vA, a);
   load_geo(slot, n3, jB, vB, b);
+  interior_slots(a, nL, vA);
+  interior_slots(b, nL, vB);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     g.sx[k] = f2(a.sx[k], b.sx[k]);
@@ -727,37 +745,40 @@ __device__ __forceinline__ void load_pair(const float4 *slot, int n3, int jA, bo
   }
 }
 
-// delta of two cells A, B (both lanes of every float2) from buffer `in`
-__device__ __forceinline__ void delta2(const GeoPair &g, float2 oh, float2 ou, float2 ov, const Buf &in,
-                                       int nL, float2 &dh, float2 &du, float2 &dv) {
-  float2 Sh = f2(0.f, 0.f), Su = f2(0.f, 0.f), Sv = f2(0.f, 0.f);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const int qA = g.nbA[k], qB = g.nbB[k];
-    if (((unsigned)qA < (unsigned)nL) & ((unsigned)qB < (unsigned)nL)) {
-      const float2 nh = f2(in.h(qA), in.h(qB));
-      const float2 nu = f2(in.u(qA), in.u(qB));
-      const float2 nv = f2(in.v(qA), in.v(qB));
-      const float2 a = g.al[k];
-      const float2 fx = g.sx[k];
-      const float2 fy = g.sy[k];
-      const float2 hf = fma2(a, sub2(oh, nh), nh);
-      const float2 uhf = fma2(a, sub2(ou, nu), nu);
-      const float2 vhf = fma2(a, sub2(ov, nv), nv);
-      const float2 Fh = fma2(uhf, fx, mul2(vhf, fy));
-      const float2 Fi = mul2(Fh, f2(rcpf(hf.x), rcpf(hf.y)));
-      const float2 hfs = mul2(mul2(f2(0.5f, 0.5f), hf), hf);
-      Sh = add2(Sh, Fh);
-      Su = fma2(uhf, Fi, fma2(hfs, fx, Su));
-      Sv = fma2(vhf, Fi, fma2(hfs, fy, Sv));
-    } else {
-      face1(Sh.x, Su.x, Sv.x, oh.x, ou.x, ov.x, in, qA, nL, g.al[k].x, g.sx[k].x, g.sy[k].x);
-      face1(Sh.y, Su.y, Sv.y, oh.y, ou.y, ov.y, in, qB, nL, g.al[k].y, g.sx[k].y, g.sy[k].y);
-    }
+// one interior face of two cells A, B (the lanes of every float2)
+__device__ __forceinline__ void face2(float2 &Sh, float2 &Su, float2 &Sv, float2 oh, float2 ou, float2 ov,
+                                      const Buf &in, int qA, int qB, float2 a, float2 fx, float2 fy) {
+  const float2 nh = f2(in.h(qA), in.h(qB));
+  const float2 nu = f2(in.u(qA), in.u(qB));
+  const float2 nv = f2(in.v(qA), in.v(qB));
+  const float2 hf = fma2(a, sub2(oh, nh), nh);
+  const float2 uhf = fma2(a, sub2(ou, nu), nu);
+  const float2 vhf = fma2(a, sub2(ov, nv), nv);
+  const float2 Fh = fma2(uhf, fx, mul2(vhf, fy));
+  const float2 Fi = mul2(Fh, f2(rcpf(hf.x), rcpf(hf.y)));
+  const float2 hfs = mul2(mul2(f2(0.5f, 0.5f), hf), hf);
+  Sh = add2(Sh, Fh);
+  Su = fma2(uhf, Fi, fma2(hfs, fx, Su));
+  Sv = fma2(vhf, Fi, fma2(hfs, fy, Sv));
+}
+
+// The face sums S of two cells A, B from buffer `in` (delta = -S; the
+// callers fold the sign into their coefficients, which is exact).  Slot 0
+// may be a wall or empty; slots 1 and 2 are interior (interior_slots).
+__device__ __forceinline__ void sums2(const GeoPair &g, float2 oh, float2 ou, float2 ov, const Buf &in, int nL,
+                                      float2 &Sh, float2 &Su, float2 &Sv) {
+  Sh = f2(0.f, 0.f);
+  Su = f2(0.f, 0.f);
+  Sv = f2(0.f, 0.f);
+  const int qA = g.nbA[0], qB = g.nbB[0];
+  if (((unsigned)qA < (unsigned)nL) & ((unsigned)qB < (unsigned)nL)) {
+    face2(Sh, Su, Sv, oh, ou, ov, in, qA, qB, g.al[0], g.sx[0], g.sy[0]);
+  } else {
+    face1(Sh.x, Su.x, Sv.x, oh.x, ou.x, ov.x, in, qA, nL, g.al[0].x, g.sx[0].x, g.sy[0].x);
+    face1(Sh.y, Su.y, Sv.y, oh.y, ou.y, ov.y, in, qB, nL, g.al[0].y, g.sx[0].y, g.sy[0].y);
   }
-  dh = f2(-Sh.x, -Sh.y);
-  du = f2(-Su.x, -Su.y);
-  dv = f2(-Sv.x, -Sv.y);
+#pragma unroll
+  for (int k = 1; k < 3; ++k) face2(Sh, Su, Sv, oh, ou, ov, in, g.nbA[k], g.nbB[k], g.al[k], g.sx[k], g.sy[k]);
 }
 
 // 4-byte cp.async global -> shared
@@ -838,7 +859,7 @@ __device__ __forceinline__ void load_tile_geo(const TileMeta &m, const float4 *g
 #pragma unroll
   for (int p = 0; p < CELLS / 2; ++p) {
     const int jA = threadIdx.x + 2 * p * TT, jB = jA + TT;
-    load_pair(slot, m.n3, jA, jA < m.n3, jB, jB < m.n3, gp[p]);
+    load_pair(slot, m.n3, m.nL, jA, jA < m.n3, jB, jB < m.n3, gp[p]);
   }
 }
 
@@ -865,7 +886,7 @@ template <int STAGE, int TT, int CELLS>
 __device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&gp)[CELLS / 2], const Buf &in,
                                       const Buf &s0, const Buf &out, float2 (&acc)[CELLS / 2][3], float c,
                                       float4 *sout, const float4 *gslot) {
-  const float2 c2 = f2(c, c);
+  const float2 nc2 = f2(-c, -c);  // delta = -S: c*delta = (-c)*S exactly
   const int lim = STAGE == 1 ? m.n3 : STAGE == 2 ? m.n2 : STAGE == 3 ? m.n1 : m.n0;
 #pragma unroll
   for (int p = 0; p < CELLS / 2; ++p) {
@@ -875,28 +896,30 @@ __device__ __forceinline__ void stage(const TileMeta &m, const GeoPair (&gp)[CEL
     const bool vB = jB0 < lim;
     const int jB = vB ? jB0 : jA;
     const float2 oh = f2(in.h(jA), in.h(jB)), ou = f2(in.u(jA), in.u(jB)), ov = f2(in.v(jA), in.v(jB));
-    float2 dh, du, dv;
-    delta2(gp[p], oh, ou, ov, in, m.nL, dh, du, dv);
+    float2 Sh, Su, Sv;
+    sums2(gp[p], oh, ou, ov, in, m.nL, Sh, Su, Sv);
     const float2 h0 = STAGE == 1 ? oh : f2(s0.h(jA), s0.h(jB));
     const float2 u0 = STAGE == 1 ? ou : f2(s0.u(jA), s0.u(jB));
     const float2 v0 = STAGE == 1 ? ov : f2(s0.v(jA), s0.v(jB));
+    // acc holds the sum of the stages' S (the negated sum of their deltas:
+    // rounding is symmetric, so the same values up to sign)
     if (STAGE < 4) {
-      const float2 xh = fma2(c2, dh, h0), xu = fma2(c2, du, u0), xv = fma2(c2, dv, v0);
+      const float2 xh = fma2(nc2, Sh, h0), xu = fma2(nc2, Su, u0), xv = fma2(nc2, Sv, v0);
       out.put(jA, xh.x, xu.x, xv.x);
       if (vB) out.put(jB, xh.y, xu.y, xv.y);
       if (STAGE == 1) {
-        acc[p][0] = dh;
-        acc[p][1] = du;
-        acc[p][2] = dv;
+        acc[p][0] = Sh;
+        acc[p][1] = Su;
+        acc[p][2] = Sv;
       } else {
-        acc[p][0] = add2(acc[p][0], dh);
-        acc[p][1] = add2(acc[p][1], du);
-        acc[p][2] = add2(acc[p][2], dv);
+        acc[p][0] = add2(acc[p][0], Sh);
+        acc[p][1] = add2(acc[p][1], Su);
+        acc[p][2] = add2(acc[p][2], Sv);
       }
     } else {
-      const float2 xh = fma2(c2, add2(acc[p][0], dh), h0);
-      const float2 xu = fma2(c2, add2(acc[p][1], du), u0);
-      const float2 xv = fma2(c2, add2(acc[p][2], dv), v0);
+      const float2 xh = fma2(nc2, add2(acc[p][0], Sh), h0);
+      const float2 xu = fma2(nc2, add2(acc[p][1], Su), u0);
+      const float2 xv = fma2(nc2, add2(acc[p][2], Sv), v0);
       sout[(int64_t)m.cell_off + jA] = make_float4(xh.x, xu.x, xv.x, 0.f);
       if (vB) sout[(int64_t)m.cell_off + jB] = make_float4(xh.y, xu.y, xv.y, 0.f);
     }
@@ -989,7 +1012,7 @@ constexpr int kPipeSmall = 768 * 2, kPipeLarge = 512 * 4;
 
 bool pipe_fits(const esr_swe_tiles *T, int shape) {
   const int max_own = shape == ESR_SWE_TILE_PIPELINED_768 ? kPipeSmall : kPipeLarge;
-  return !T->exact && T->max_own <= max_own && T->max_local <= pipe::kMaxLocal;
+  return !T->exact && T->max_own <= max_own && T->max_local <= pipe::kMaxLocal && T->slot_info == 1;
 }
 
 int pipe_shape(const esr_swe_tiles *) { return ESR_SWE_TILE_PIPELINED_512; }
@@ -1088,8 +1111,9 @@ extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, do
   if (kernel == ESR_SWE_TILE_PIPELINED) kernel = pipe_shape(tiles);
   if (kernel == ESR_SWE_TILE_PIPELINED_512 || kernel == ESR_SWE_TILE_PIPELINED_768) {
     if (!pipe_fits(tiles, kernel))
-      return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, <= 4096 local cells a "
-                                            "tile and <= 2048 own cells (512-thread shape) or <= 1536 (768-thread)");
+      return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, slot_info == 1, <= 4096 "
+                                            "local cells a tile and <= 2048 own cells (512-thread shape) or <= 1536 "
+                                            "(768-thread)");
   } else if (kernel != ESR_SWE_TILE_BLOCKED) {
     return esr::fail(ESR_ERR_ARG, "unknown tile kernel");
   }

@@ -254,7 +254,7 @@ class SweEngine:
                                         st["max_own"], st["max_halo3"], _lib.ptr(self.tile_meta),
                                         _lib.ptr(self.tile_off3), _lib.ptr(self.tile_offh), _lib.ptr(self.tile_halo),
                                         _lib.ptr(self.t_slots), _lib.ptr(self.t_area), _lib.ptr(self.t_inv_area),
-                                        exact, st["max_halo"])
+                                        exact, st["slot_info"])
 
     def set_precision(self, precision: str) -> None:
         """Switch between 'exact' and 'fast' arithmetic (same layout)."""
@@ -458,6 +458,21 @@ def _slots_by_neighbour(meta: np.ndarray, off3: np.ndarray, lnbr: np.ndarray) ->
     return order
 
 
+def _one_boundary_slot(meta: np.ndarray, lnbr: np.ndarray) -> bool:
+    """True when no tile cell has more than one wall or empty face slot, so
+    in the fast layout (records sorted by neighbour, negatives first) slots
+    1 and 2 of every cell are interior faces."""
+    n3 = meta[:, 4].astype(np.int64)
+    total = int(n3.sum())
+    if total == 0:
+        return True
+    tile = np.repeat(np.arange(n3.shape[0], dtype=np.int64), n3)
+    j = np.arange(total, dtype=np.int64) - np.repeat(np.cumsum(n3) - n3, n3)
+    off3 = np.concatenate([[0], np.cumsum(n3)[:-1]])
+    idx = 3 * off3[tile] + np.arange(3, dtype=np.int64)[:, None] * n3[tile] + j
+    return bool(((lnbr[idx] < 0).sum(axis=0) <= 1).all())
+
+
 def tile_layout(nbr: np.ndarray, part: np.ndarray) -> dict:
     """Tiled face-slot layout (see ``esr_swe_tiles`` in include/esr_gb300.h).
 
@@ -488,7 +503,7 @@ def tile_layout(nbr: np.ndarray, part: np.ndarray) -> dict:
     cum = meta[:, 1:6].astype(np.int64)
     max_own, max_l3, max_local = int(cum[:, 0].max()), int(cum[:, 3].max()), int(cum[:, 4].max())
     stats = dict(ntiles=ntiles, max_own=max_own, max_l3=max_l3, max_local=max_local,
-                 max_halo3=int((cum[:, 3] - cum[:, 0]).max()), max_halo=int((cum[:, 4] - cum[:, 0]).max()),
+                 max_halo3=int((cum[:, 3] - cum[:, 0]).max()), slot_info=int(_one_boundary_slot(meta, lnbr)),
                  mean_own=float(cum[:, 0].mean()), l3_over_own=float(t3.value / nc),
                  local_over_own=float(cum[:, 4].sum() / nc), smem=(3 * max_local + 6 * max_l3) * 4)
     return dict(meta=meta, off3=off3, offh=offh, halo=halo[:th.value], lnbr=lnbr, slot_src=slot_src,

@@ -326,7 +326,10 @@ typedef struct {
   const void *area;     /* [sum(n3)], read when exact != 0 */
   const void *inv_area; /* not read (reserved) */
   int32_t exact;        /* as in esr_swe_mesh */
-  int32_t max_halo;     /* max nL - n0 (informational; not read) */
+  int32_t slot_info;    /* 1: no cell has more than one wall or empty face
+                         * slot, so with exact == 0 (each cell's records
+                         * sorted by lnbr) slots 1 and 2 are interior
+                         * faces; else 0.  The pipelined kernel needs 1. */
 } esr_swe_tiles;
 
 /* Shared memory one CTA of esr_swe_tile_step uses, or -1 if the layout is
@@ -358,7 +361,8 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
  *     thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
  *     n0 <= 2048) and PIPELINED_768 (768 threads x 2, n0 <= 1536); cells
  *     of level <= 3 past those read their records per stage.  PIPELINED is
- *     the 512-thread shape.  Needs nL <= 4096 in every tile.
+ *     the 512-thread shape.  Needs nL <= 4096 in every tile and
+ *     slot_info == 1.
  * AUTO picks a pipelined shape when the layout allows it. */
 #define ESR_SWE_TILE_AUTO 0
 #define ESR_SWE_TILE_BLOCKED 1

@@ -85,7 +85,8 @@ def _tile_layout_numpy(nbr: np.ndarray, part: np.ndarray) -> dict:
     meta[:, 1:6] = cum
     max_own, max_l3, max_local = int(cum[:, 0].max()), int(cum[:, 3].max()), int(cum[:, 4].max())
     stats = dict(ntiles=ntiles, max_own=max_own, max_l3=max_l3, max_local=max_local,
-                 max_halo3=int((cum[:, 3] - cum[:, 0]).max()), max_halo=int((cum[:, 4] - cum[:, 0]).max()),
+                 max_halo3=int((cum[:, 3] - cum[:, 0]).max()), slot_info=int(all(int((lnbr[3 * off3[t] + np.arange(3) * cum[t, 3] + jj] < 0).sum()) <= 1
+                                   for t in range(ntiles) for jj in range(cum[t, 3]))),
                  mean_own=float(counts.mean()), l3_over_own=float(total3 / nc),
                  local_over_own=float(cum[:, 4].sum() / nc), smem=(3 * max_local + 6 * max_l3) * 4)
     return dict(meta=meta, off3=off3, offh=offh, halo=halo, lnbr=lnbr, slot_src=slot_src, area_src=area_src,
