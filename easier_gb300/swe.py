@@ -112,7 +112,115 @@ def bind(m) -> Optional[dict]:
         return None
     if s["gather_src"]._idx_max >= nc:
         return None
-    return dict(tensors=t, selectors=s, reducers=r, nc=nc, ne=ne, nbc=nbc, dtype=dtype)
+    return dict(tensors=t, selectors=s, reducers=r, nc=nc, ne=ne, nbc=nbc, dtype=dtype, dt_attr="dt")
+
+
+def find_roles(m) -> Optional[dict]:
+    """Role binding of a shallow-water module whose attributes are not named
+    like the tutorial's, found from its structure and checked on its own
+    forward.
+
+    Structure: two sum Reducers onto the same n cells (the longer index =
+    the interior edges' destinations, the shorter = the wall cells), a
+    Selector with each of their indices (gather of the destination cell /
+    of the wall cell) and one more Selector over the edges (the source
+    cell); three float edge tensors, two wall tensors, cell tensors and a
+    float step size among the module's attributes.  The three cell tensors
+    forward() writes are the state.  Every assignment of the remaining
+    roles (state order, area, the edge and wall tensors' order, dt) is then
+    run through one step of the staged fused kernel in exact arithmetic and
+    compared bit for bit with one step of forward() from the same random
+    state; the binding is the first assignment that matches, or None."""
+    import itertools
+    sels = [v for v in m._modules.values() if isinstance(v, _m.Selector)]
+    reds = [v for v in m._modules.values() if isinstance(v, _m.Reducer)]
+    if len(sels) != 3 or len(reds) != 2 or any(r.reduce != "sum" for r in reds) or reds[0].n != reds[1].n:
+        return None
+    if any(getattr(x, "easier_index_status", None) != "rewritten" for x in sels + reds):
+        return None
+    nc = reds[0].n
+    scat, scat_b = sorted(reds, key=lambda r: -r.idx.shape[0])
+    ne, nbc = scat.idx.shape[0], scat_b.idx.shape[0]
+    if ne == nbc:
+        return None
+    g_dst = [x for x in sels if x.idx.shape[0] == ne and torch.equal(x.idx, scat.idx)]
+    g_b = [x for x in sels if x.idx.shape[0] == nbc and torch.equal(x.idx, scat_b.idx)]
+    if not g_dst or not g_b:
+        return None
+    g_src = [x for x in sels if x is not g_dst[0] and x is not g_b[0] and x.idx.shape[0] == ne]
+    if len(g_src) != 1 or g_src[0]._idx_max >= nc:
+        return None
+    params = [v for v in m._parameters.values() if isinstance(v, _m.Tensor) and v.is_partition and v.dim() == 1]
+    dtype = next((v.dtype for v in params if v.shape[0] == nc), None)
+    if dtype not in (torch.float32, torch.float64):
+        return None
+    of = lambda n: [v for v in params if v.shape[0] == n and v.dtype == dtype]  # noqa: E731
+    cells, edges, walls = of(nc), of(ne), of(nbc)
+    dts = [(k, v) for k, v in vars(m).items() if isinstance(v, float) and not k.startswith("_")]
+    if len(cells) < 4 or len(edges) != 3 or len(walls) != 2 or not dts or cells[0].device.type != "cuda":
+        return None
+    dev = cells[0].device
+    saved = [(v, v.data) for v in cells]
+    gen = torch.Generator(device="cpu").manual_seed(4321)
+    try:
+        # which cell tensors forward() writes: the state
+        for v in cells:
+            v.data = (1.0 + 0.05 * torch.rand(nc, generator=gen, dtype=torch.float64)).to(dtype).to(dev)
+        before = [v.data.clone() for v in cells]
+        type(m).forward(m)
+        state = [v for v, b in zip(cells, before) if not torch.equal(v.data, b)]
+        if len(state) != 3:
+            return None
+        for v, d in saved:
+            v.data = d
+        # the reference step: forward() from a random state
+        inputs = [(1.0 + 0.05 * torch.rand(nc, generator=gen, dtype=torch.float64)).to(dtype).to(dev)
+                  for _ in state]
+        for v, x in zip(state, inputs):
+            v.data = x.clone()
+        type(m).forward(m)
+        ref = [v.data.clone() for v in state]
+    except Exception:  # not a forward we can run this way
+        return None
+    finally:
+        for v, d in saved:
+            v.data = d
+    src = g_src[0].idx.cpu().numpy().astype(np.int64)
+    dst = g_dst[0].idx.cpu().numpy().astype(np.int64)
+    bcell = g_b[0].idx.cpu().numpy().astype(np.int64)
+    lay = cell_layout(nc, src, dst, bcell, reorder="none")
+    pos = torch.from_numpy(lay["pos"]).to(dev)
+    nbr = torch.from_numpy(lay["nbr"]).to(dev)
+    valid = pos >= 0
+    safe = torch.where(valid, pos, torch.zeros_like(pos))
+    zero = torch.zeros(1, dtype=dtype, device=dev)
+    ws = torch.empty(3 * 4 * nc, dtype=dtype, device=dev)
+    others = [v for v in cells if not any(v is x for x in state)]
+    for order in itertools.permutations(range(3)):
+        for area in others:
+            for e in itertools.permutations(edges):
+                for w in itertools.permutations(walls):
+                    fx = torch.where(valid, torch.cat([e[0].data, w[0].data])[safe], zero).contiguous()
+                    fy = torch.where(valid, torch.cat([e[1].data, w[1].data])[safe], zero).contiguous()
+                    al = torch.where(valid, torch.cat([e[2].data, torch.zeros(nbc, dtype=dtype, device=dev)])[safe],
+                                     zero).contiguous()
+                    ar = area.data.contiguous()
+                    mesh_d = _lib.SweMesh(nc, lay["width"], _lib.dtype_code(dtype), _lib.ptr(nbr), _lib.ptr(fx),
+                                          _lib.ptr(fy), _lib.ptr(al), _lib.ptr(ar), _lib.ptr(ar), 1, 0)
+                    for dt_name, dt in dts:
+                        st = torch.zeros((nc, 4), dtype=dtype, device=dev)
+                        for j in range(3):
+                            st[:, j] = inputs[order[j]]
+                        _lib.call("esr_swe_step", ctypes.byref(mesh_d), float(dt), _lib.ptr(st), 1, _lib.ptr(ws),
+                                  _lib.stream_handle(dev))
+                        if all(torch.equal(st[:, j], ref[order[j]]) for j in range(3)):
+                            t = dict(zip(STATE, (state[i] for i in order)))
+                            t.update(area=area, sx=e[0], sy=e[1], alpha=e[2], bsx=w[0], bsy=w[1])
+                            return dict(tensors=t, selectors=dict(gather_src=g_src[0], gather_dst=g_dst[0],
+                                                                  gather_b=g_b[0]),
+                                        reducers=dict(scatter=scat, scatter_b=scat_b), nc=nc, ne=ne, nbc=nbc,
+                                        dtype=dtype, dt_attr=dt_name)
+    return None
 
 
 class SweEngine:
@@ -132,6 +240,7 @@ class SweEngine:
         self.tile_cells = min(tile_cells or DEFAULT_TILE_CELLS or self._auto_tile_cells(), TILE_CELLS)
         self.mode = mode
         self.tile_kernel = DEFAULT_TILE_KERNEL
+        self._dt_attr = binding.get("dt_attr", "dt")
         self._build_layout()
 
     def _auto_tile_cells(self) -> int:
@@ -310,12 +419,12 @@ class SweEngine:
         if self.tiled:
             a, b = self.bufs[self.cur], self.bufs[1 - self.cur]
             _lib.call("esr_swe_tile_step_with", ctypes.byref(self._tiles), _TILE_KERNELS[self.tile_kernel],
-                      float(self.m.dt), _lib.ptr(a), _lib.ptr(b), int(steps), stream)
+                      self.dt, _lib.ptr(a), _lib.ptr(b), int(steps), stream)
             if steps % 2:
                 self.cur = 1 - self.cur
                 self._bind_views()
         else:
-            _lib.call("esr_swe_step", ctypes.byref(self._mesh), float(self.m.dt), _lib.ptr(self.state), int(steps),
+            _lib.call("esr_swe_step", ctypes.byref(self._mesh), self.dt, _lib.ptr(self.state), int(steps),
                       _lib.ptr(self.ws), stream)
 
     def forward(self):
@@ -344,6 +453,11 @@ class SweEngine:
                   f" local/own={st['local_over_own']:.3f} smem={st['smem']}"
                   f" cta={self.tile_threads()} kernel={self.tile_kernel_name()}")
         return s
+
+    @property
+    def dt(self) -> float:
+        """The module's step size (read at every step, as its forward does)."""
+        return float(getattr(self.m, self._dt_attr))
 
     def tile_kernel_name(self) -> str:
         """The tile kernel step() runs: 'pipelined_512', 'pipelined_768' or
@@ -580,7 +694,10 @@ def try_install(m, modules: List, mode: Optional[str] = None, precision: Optiona
     precision = precision or DEFAULT_PRECISION
     binding = bind(m)
     if binding is None:
-        return None
+        binding = find_roles(m)
+        if binding is None:
+            return None
+        logger.info(f"{type(m).__name__}: shallow-water roles found from its structure")
     reorder = "none" if _shared_with_others(m, modules) else "rcm"
     if reorder == "none" and mode == "auto":
         mode = "staged"

@@ -235,3 +235,86 @@ def test_pipelined_tile_kernel_equals_blocked_kernel_bitwise(n, target, monkeypa
     assert ops.device_status() == 0
     for o in outs[1:]:
         assert torch.equal(outs[0], o)
+
+
+def _renamed_swe(n, dt, dtype):
+    """The tutorial's shallow-water module with every attribute renamed and
+    the geometry tensors declared in another order: the fused engine must
+    find the roles from the module's structure."""
+    from easier_gb300 import mesh
+
+    class Renamed(esr.Module):
+        def __init__(self):
+            super().__init__()
+            m = mesh.triangular_mesh(n)
+            g = mesh.swe_geometry(m)
+            t = lambda a: torch.as_tensor(a)  # noqa: E731
+            self.step_size = dt
+            self.label = 3.5   # another float attribute: not the step size
+            self.to_cell = esr.Reducer(t(m.dst), m.nc)
+            self.take_a = esr.Selector(t(m.src))
+            self.take_b = esr.Selector(t(m.dst))
+            self.to_cell_w = esr.Reducer(t(m.bcells), m.nc)
+            self.take_w = esr.Selector(t(m.bcells))
+            f = torch.float64
+            self.cx = esr.Tensor(t(g.x).to(f), mode="partition")
+            self.w_ny = esr.Tensor(t(g.bsy).to(f), mode="partition")
+            self.vol = esr.Tensor(t(g.area).to(f), mode="partition")
+            self.weight = esr.Tensor(t(g.alpha).to(f), mode="partition")
+            self.ny = esr.Tensor(t(g.sy).to(f), mode="partition")
+            self.w_nx = esr.Tensor(t(g.bsx).to(f), mode="partition")
+            self.nx = esr.Tensor(t(g.sx).to(f), mode="partition")
+            self.cy = esr.Tensor(t(g.y).to(f), mode="partition")
+            self.q = esr.Tensor(esr.zeros((m.nc,), dtype=f), mode="partition")
+            self.depth = esr.Tensor(t(mesh.gaussian_bump(g.x, g.y)).to(f), mode="partition")
+            self.p = esr.Tensor(esr.zeros((m.nc,), dtype=f), mode="partition")
+
+        def face(self, phi):
+            return (1 - self.weight) * self.take_a(phi) + self.weight * self.take_b(phi)
+
+        def rate(self, h, uh, vh):
+            h_f, uh_f, vh_f = self.face(h), self.face(uh), self.face(vh)
+            u_f = uh_f / h_f
+            v_f = vh_f / h_f
+            hsq = 0.5 * h_f * h_f
+            a = uh_f * self.nx
+            b = vh_f * self.ny
+            wall = 0.5 * self.take_w(h) ** 2
+            dh = -(self.to_cell(a + b)) / self.vol
+            du = -(self.to_cell((u_f * uh_f + hsq) * self.nx + u_f * b) + self.to_cell_w(wall * self.w_nx)) / self.vol
+            dv = -(self.to_cell(v_f * a + (v_f * vh_f + hsq) * self.ny) + self.to_cell_w(wall * self.w_ny)) / self.vol
+            return dh, du, dv
+
+        def forward(self):
+            k, h, p, q = self.step_size, self.depth, self.p, self.q
+            a1, b1, c1 = self.rate(h, p, q)
+            a2, b2, c2 = self.rate(h + 0.5 * k * a1, p + 0.5 * k * b1, q + 0.5 * k * c1)
+            a3, b3, c3 = self.rate(h + 0.5 * k * a2, p + 0.5 * k * b2, q + 0.5 * k * c2)
+            a4, b4, c4 = self.rate(h + k * a3, p + k * b3, q + k * c3)
+            self.depth[:] += k / 6 * (a1 + a2 + a3 + a4)
+            self.p[:] += k / 6 * (b1 + b2 + b3 + b4)
+            self.q[:] += k / 6 * (c1 + c2 + c3 + c4)
+
+    mod = Renamed()
+    if dtype != torch.float64:
+        mod.to(dtype)
+    return mod
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_engine_finds_roles_of_a_renamed_module(dtype):
+    """A module with the tutorial's step under other attribute names gets the
+    fused engine (roles found from its structure, checked on its own
+    forward) and steps bit for bit like the tutorial module."""
+    n, dt, steps = 30, 5e-4, 6
+    ren = _renamed_swe(n, dt, dtype)
+    [ren] = esr.compile([ren], "cuda")
+    assert getattr(ren, "easier_fused_engine", None) is not None
+    for _ in range(steps):
+        ren()
+    tut = workloads.make_swe(n, dt=dt, dtype=dtype)
+    [tut] = esr.compile([tut], "cuda")
+    for _ in range(steps):
+        tut()
+    for a, b in (("depth", "h"), ("p", "uh"), ("q", "vh")):
+        assert torch.equal(getattr(ren, a).collect().cpu(), getattr(tut, b).collect().cpu()), a
