@@ -380,7 +380,7 @@ def bench_swe(args, world, rank, local):
         "engine": eng.describe(),
         "setup_s": {"mesh_geometry_and_module": t_mesh,
                     "compile": t_compile,
-                    "compile_note": "layout on the host: RCM, BFS-bisection tiles, tile/halo lists; and the "
+                    "compile_note": "layout on the host: BFS-bisection tiles, tile/halo lists; and the "
                                     "compile-time check of one fused step against the module's own forward"},
         "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
                    "state within 1e-5 (FP32) relative max-norm of the FP64 oracle (N=100 x 1,000 steps, N=2000 x 5 "

@@ -62,8 +62,9 @@ TILE_SMEM = 227 * 1024  # shared memory per CTA
 DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
 # Numbering before the tile partition of a tiled layout: "rcm" (reverse
 # Cuthill-McKee, then tile-major) or "tiles" (the module's own order, then
-# tile-major: the partition alone, without the RCM pass)
-TILED_REORDER = "rcm"
+# tile-major: the partition alone, without the RCM pass).  Measured at
+# N=2000: the same kernel time (0.454 vs 0.457 ms), 2 s less compile.
+TILED_REORDER = "tiles"
 # Fast arithmetic on large meshes: tiles for the pipelined tile kernel
 # (<= 2048 own cells, <= 4096 local cells)
 PIPE_TILE_TARGET = 1900
@@ -267,6 +268,7 @@ class SweEngine:
         pipe_tries = 0
         while True:
             reorder = TILED_REORDER if (want_tiles and self.reorder == "rcm") else self.reorder
+            self.layout_order = reorder if want_tiles else self.reorder
             lay = cell_layout(nc, src, dst, bcell, reorder=reorder,
                               tile_cells=tile_cells if want_tiles else None)
             if lay["part"] is None:
@@ -446,7 +448,8 @@ class SweEngine:
 
     def describe(self) -> str:
         s = (f"nc={self.nc} width={self.width} dtype={str(self.dtype).replace('torch.', '')} "
-             f"kernel={'tiled' if self.tiled else 'staged'} precision={self.precision} reorder={self.reorder}")
+             f"kernel={'tiled' if self.tiled else 'staged'} precision={self.precision} "
+             f"reorder={self.reorder if not self.tiled else ('rcm+tiles' if self.layout_order == 'rcm' else 'tiles')}")
         if self.tiled:
             st = self.tile_stats
             s += (f" tiles={st['ntiles']} own<={st['max_own']} L3/own={st['l3_over_own']:.3f}"
