@@ -290,6 +290,8 @@ def bench_swe(args, world, rank, local):
     eng = eqn.easier_fused_engine
     if eng is None:
         raise RuntimeError("the fused shallow-water engine was not installed")
+    if args.tile_kernel:  # this engine only (the exact-arithmetic figures keep theirs)
+        eng.tile_kernel = args.tile_kernel
     nc = eng.nc
     stream = torch.cuda.current_stream(dev)
     eng.step(args.warmup)
@@ -667,17 +669,23 @@ def gnn_row_bytes(slots_per_row: float) -> float:
     return 4 * (128 + 12 * slots_per_row) + 20
 
 
+POLY_DEGREE = 4  # the polynomial-Jacobi control of the GNN line
+
+
 def bench_gnn(args, world, rank, local):
-    """Flexible CG with the GNN preconditioner against Jacobi-PCG, both
-    batched and df64, on held-out seeded instances."""
-    from easier_gb300.numeric.batched import BatchedPCG, p1_instances
+    """Flexible CG with the GNN preconditioner against Jacobi-PCG and
+    against a degree-4 polynomial-Jacobi PCG (five damped Jacobi sweeps per
+    application, four of them SpMVs), all batched and df64, on held-out
+    seeded instances."""
+    from easier_gb300.numeric.batched import BatchedPCG, POLY_OMEGA, p1_instances
     from easier_gb300.numeric.preconditioner.gnn import GnnWeights, WEIGHTS_FILE
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     insts = p1_instances(args.count, args.nmin, args.nmax, seed=args.seed)
     stream = torch.cuda.current_stream(dev)
     out = {}
-    for name, kw in (("jacobi", {}), ("gnn", {"gnn": GnnWeights.load()})):
+    for name, kw in (("jacobi", {}), ("poly_jacobi", {"poly_degree": POLY_DEGREE}),
+                     ("gnn", {"gnn": GnnWeights.load()})):
         eng = BatchedPCG(insts, jacobi=True, precision="df64", device=dev, graph_iters=args.chunk, **kw)
         eng.autotune()
         x0 = torch.zeros_like(eng.b64)
@@ -721,7 +729,8 @@ def bench_gnn(args, world, rank, local):
                      "launches": eng.kernel_launches - l0, "clocks": clk.summary()}
         del eng
         torch.cuda.empty_cache()
-    g, j = out["gnn"], out["jacobi"]
+    g, j, pj = out["gnn"], out["jacobi"], out["poly_jacobi"]
+    pj["degree"], pj["omega"] = POLY_DEGREE, POLY_OMEGA
     peak, peak_kind = _peaks()
     return {
         "metric": "Poisson solves/s (batched, GNN-preconditioned flexible CG)", "value": g["solves_per_s"],
@@ -732,7 +741,9 @@ def bench_gnn(args, world, rank, local):
         "config": batched_config(args, world),
         "solve": {"gnn": {k: v for k, v in g.items() if k != "clocks"},
                   "jacobi": {k: v for k, v in j.items() if k != "clocks"},
-                  "gnn_over_jacobi_solves_per_s": g["solves_per_s"] / j["solves_per_s"]},
+                  "poly_jacobi": {k: v for k, v in pj.items() if k != "clocks"},
+                  "gnn_over_jacobi_solves_per_s": g["solves_per_s"] / j["solves_per_s"],
+                  "gnn_over_poly_jacobi_solves_per_s": g["solves_per_s"] / pj["solves_per_s"]},
         "roofline": {"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": g["achieved_gbs"] / peak, "peak_kind": peak_kind, "traffic": None,
                      "bytes_model": "df64 CG bytes per packed row-iteration (engine model) plus, per GNN "
@@ -749,9 +760,9 @@ def solver_secondaries(args, world, rank, local):
     P1-1000 Jacobi-PCG in FP64 and double-float (3 timed solves each), the
     tutorial's FV Poisson at N=500 with its CG (3 timed solves), the
     256-instance batch in double-float (one timed one-launch batch solve)
-    and GNN flexible CG against Jacobi-PCG on the held-out batch (one timed
-    batch each).  Each keeps its own CUDA-event timing, FP64-verified
-    residuals, roofline and clock record."""
+    and GNN flexible CG against Jacobi-PCG and polynomial-Jacobi PCG on the
+    held-out batch (one timed batch each).  Each keeps its own CUDA-event
+    timing, FP64-verified residuals, roofline and clock record."""
     import copy
     out = {}
     runs = (("poisson_p1_1000_fp64", bench_poisson, dict(workload="poisson", n=1000, precision="native", steps=3,
@@ -961,6 +972,9 @@ def main():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-solvers", action="store_true", help="swe: leave out the solver figures")
     ap.add_argument("--tile-cells", type=int, default=None, help="swe: target cells per tile (FP32 tiled step)")
+    ap.add_argument("--tile-kernel", default=None,
+                    choices=["auto", "blocked", "pipelined", "pipelined_512", "pipelined_768", "pipelined_1024"],
+                    help="swe: tile kernel of the FP32 tiled step")
     args = ap.parse_args()
     if args.n is None:
         args.n = {"swe": 2000, "poisson-fv": 500}.get(args.workload, 1000)

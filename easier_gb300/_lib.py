@@ -71,7 +71,7 @@ class Batch(Structure):
                 ("col", c_void_p), ("val", c_void_p), ("diag", c_void_p), ("invdiag", c_void_p),
                 ("val64", c_void_p), ("diag64", c_void_p), ("block_inst", c_void_p), ("inst_block0", c_void_p),
                 ("chunk_tile0", c_void_p), ("chunk_inst", c_void_p), ("inst_chunk0", c_void_p),
-                ("gnn", POINTER(Gnn))]
+                ("gnn", POINTER(Gnn)), ("poly_tmp", c_void_p), ("poly_degree", c_int32), ("pad_poly_", c_int32)]
 
 
 class BcgInst(Structure):
@@ -149,7 +149,7 @@ _SIGS = {
     "esr_gmres_read": (c_int, [_P, POINTER(GmresScalars), _P]),
 }
 
-ABI_VERSION = 10
+ABI_VERSION = 11
 
 
 def library_path() -> Path:

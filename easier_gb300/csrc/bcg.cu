@@ -31,6 +31,13 @@
 //           significand bits on the FP32 pipes (GB300's FP64 rate is 1/59 of
 //           its FP32 rate, and the FP64 CG saturates the FP64 pipe before
 //           HBM).
+// Polynomial-Jacobi preconditioner (esr_batch.poly_degree = d > 0; a
+// classical control for the GNN, no reference counterpart): z = M r is the
+// result of d+1 damped Jacobi sweeps on A z = r from z = 0 (a Neumann
+// polynomial of degree d in W A, W = omega/diag, held in invdiag).  The
+// kernels that write r (init, update, replacement) write the first sweep
+// z = W r; bcg_poly_kernel runs the other d at the start of the next
+// iteration, the last of them finishing r.z and beta.
 // Convergence is re-checked on the FP64 true residual b - A x computed from
 // an FP64 copy of the matrix (esr_bcg_verify).  An instance whose true
 // residual misses the tolerance continues from it: r = b - A x replaces the
@@ -325,9 +332,56 @@ bcg_update_kernel(BArgs a, const typename P::V *__restrict__ invdiag, typename P
             s.rr_mark = tot[0];
           }
         }
-      } else {
+      } else if (!a.poly) {  // polynomial: beta and r.z follow the sweeps
         set_beta(s, tot[1] / s.rz);
         s.rz = tot[1];
+      }
+    }
+  }
+}
+
+// ---- polynomial-Jacobi sweep: y_out = y_in + W (r - A y_in), persistent
+// over the running chunks.  Each row reads other rows' y_in (never written
+// here) and writes only its own y_out.  The last sweep (y_out = z) adds r.z
+// per instance and sets beta = r.z / r.z_old, except for a first direction
+// (refresh != 0: after init), which only takes r.z.  After a residual
+// replacement the direction continues (refresh == 0) with the r.z_old of
+// the iteration before it.
+template <class P, bool LAST>
+__global__ void __launch_bounds__(kBThreads, 4)
+bcg_poly_kernel(BArgs a, const typename P::V *__restrict__ val, const typename P::V *__restrict__ diag,
+                const typename P::V *__restrict__ w, const typename P::V *__restrict__ r,
+                const typename P::V *__restrict__ y_in, typename P::V *__restrict__ y_out, BcgLayout L) {
+  using V = typename P::V;
+  const int count = L.head->acount;
+  for (int u = blockIdx.x; u < count; u += gridDim.x) {
+    const int c = L.alist[u];
+    const int inst = a.chunk_inst[c];
+    if (L.inst[inst].done) continue;
+    typename P::Acc rz;
+    const int t1 = a.chunk_tile0[c + 1];
+#pragma unroll 2
+    for (int t = a.chunk_tile0[c]; t < t1; ++t) {
+      const int64_t i = (int64_t)t * kBThreads + threadIdx.x;
+      const V yi = y_in[i];
+      const V ri = r[i];
+      const V ay = P::fma(diag[i], yi, bsell_row<P>(i, a.n, a.slice_ptr, a.col, val, y_in));
+      const V yo = P::fma(w[i], P::sub(ri, ay), yi);
+      y_out[i] = yo;
+      if constexpr (LAST) rz.add(ri, yo);
+    }
+    if constexpr (LAST) {
+      const double v[1] = {bsum<kBThreads>(rz)};
+      double tot[1];
+      if (chunk_finish<1>(a, c, inst, v, L, tot) && threadIdx.x == 0) {
+        esr_bcg_inst &s = L.inst[inst];
+        if (!(tot[0] != 0.0) || !isfinite(tot[0])) {
+          s.done = 3;  // breakdown (M r = 0 or not finite)
+          retire(L);
+        } else {
+          if (s.refresh == 0) set_beta(s, tot[0] / s.rz);
+          s.rz = tot[0];
+        }
       }
     }
   }
@@ -370,7 +424,11 @@ bcg_residual_kernel(BArgs a, const double *__restrict__ val64, const double *__r
 }
 
 // ---- pass 3, instances whose true residual missed: residual replacement
-// r = r64, z = M r, beta = r.z / r.z_old, p = z + beta p; running again
+// r = r64, z = M r, then p = z + beta p with beta = r.z / r.z_old while the
+// true residual is within twice the recurrence residual (rounding drift:
+// the direction stays conjugate enough to keep), else a restart, p = z (a
+// residual far from the recurrence's makes beta huge and the continued
+// direction useless); running again
 template <class P>
 __global__ void __launch_bounds__(kBThreads)
 bcg_replace_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const double *__restrict__ r64,
@@ -391,12 +449,15 @@ bcg_replace_kernel(BArgs a, const typename P::V *__restrict__ invdiag, const dou
   const double v[1] = {bsum<kBThreads>(rz)};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
-    // GNN mode: p restarts from the Jacobi direction (beta = 0)
-    set_beta(st, (st.mode != kModeGnn && st.rz != 0.0) ? tot[0] / st.rz : 0.0);
-    st.rz = tot[0];
-    st.rz_jac = tot[0];
+    // GNN mode: p restarts from the Jacobi direction
+    const bool restart = st.mode == kModeGnn || st.rz == 0.0 || !(st.true_rr <= 4.0 * st.rr);
+    if (!a.poly) {  // polynomial: z = W r is the first sweep; r.z_old stays for the last
+      set_beta(st, restart ? 0.0 : tot[0] / st.rz);
+      st.rz = tot[0];
+      st.rz_jac = tot[0];
+    }
     st.rr = st.true_rr;
-    st.verified = -2;  // p update pending
+    st.verified = restart ? -3 : -2;  // p update pending
   }
 }
 
@@ -405,13 +466,15 @@ __global__ void __launch_bounds__(kBThreads)
 bcg_replace_p_kernel(BArgs a, typename P::V *__restrict__ z, typename P::V *__restrict__ p, BcgLayout L) {
   const int inst = a.block_inst[blockIdx.x];
   esr_bcg_inst &st = L.inst[inst];
-  if (st.verified != -2) return;
+  if (st.verified != -2 && st.verified != -3) return;
   const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
-  // the continued direction p_new = z + beta p, in p (for bcg_spmv_kernel)
-  // and in z (for bcg_pq_kernel's first direction), so the next product is
-  // q = A p_new exactly (the update recomputes z from r before anything
-  // else reads it)
-  if (i < a.n) {
+  // the continued direction p_new = z + beta p (beta = 0 on a restart), in
+  // p (for bcg_spmv_kernel) and in z (for bcg_pq_kernel's first direction),
+  // so the next product is q = A p_new exactly (the update recomputes z
+  // from r before anything else reads it)
+  // (polynomial: p stays; the sweeps finish z and beta, and the next
+  // direction continues from p as in any iteration, or starts at p = z)
+  if (i < a.n && !a.poly) {
     const typename P::V pn = P::fma(P::beta(st), p[i], z[i]);
     p[i] = pn;
     z[i] = pn;
@@ -421,7 +484,7 @@ bcg_replace_p_kernel(BArgs a, typename P::V *__restrict__ z, typename P::V *__re
   const double v[1] = {0.0};
   double tot[1];
   if (tile_finish<1>(a, inst, v, L, tot) && threadIdx.x == 0) {
-    st.refresh = 2;
+    st.refresh = (a.poly && st.verified == -2) ? 0 : 2;
     st.verified = 0;
     st.restarts += 1;
     st.done = 0;
@@ -474,7 +537,24 @@ int run_iterate(const esr_batch *B, void *x, void *r, void *z, void *p, void *q,
   BcgLayout L = layout_of(ws, B->ninst, B->nchunks);
   const BArgs a = bargs(B);
   bcg_compact_kernel<<<1, 1024, 0, s>>>(a, L);
+  const int d = B->poly_degree;
+  V *const tmp0 = (V *)B->poly_tmp, *const tmp1 = tmp0 ? tmp0 + B->n : nullptr;
   for (int32_t it = 0; it < k; ++it) {
+    if (d > 0) {  // z = M r: sweeps 2..d+1 (z -> tmp0 -> tmp1 -> tmp0 ... -> z)
+      const V *src = (const V *)z;
+      for (int j = 1; j <= d; ++j) {
+        V *dst = j == d ? (V *)z : ((j & 1) ? tmp0 : tmp1);
+        if (j == d)
+          bcg_poly_kernel<P, true><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag,
+                                                                 (const V *)B->invdiag, (const V *)r, src, dst, L);
+        else
+          bcg_poly_kernel<P, false><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag,
+                                                                  (const V *)B->invdiag, (const V *)r, src, dst, L);
+        src = dst;
+      }
+      if constexpr (!P::kFusedDirection)
+        bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
+    }
     if constexpr (P::kFusedDirection)
       bcg_pq_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->val, (const V *)B->diag, (const V *)z, (V *)p,
                                                      (V *)q, L);
@@ -489,7 +569,7 @@ int run_iterate(const esr_batch *B, void *x, void *r, void *z, void *p, void *q,
       bcg_zfix_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)B->invdiag, (const V *)r, (V *)z, L);
     }
     if constexpr (!P::kFusedDirection)
-      bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
+      if (d == 0) bcg_pupdate_kernel<P><<<B->grid, kBThreads, 0, s>>>(a, (const V *)z, (V *)p, L);
   }
   ESR_LAUNCH_CHECK("esr_bcg_iterate");
   return ESR_OK;

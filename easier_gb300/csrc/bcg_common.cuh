@@ -279,12 +279,13 @@ struct BArgs {
   const int32_t *inst_rows;  // GNN only: rows before padding
   int32_t use_gnn;
   int32_t stall_window;
+  int32_t poly;  // polynomial-Jacobi: z, r.z and beta come from bcg_poly_kernel
 };
 
 inline BArgs bargs(const esr_batch *B) {
   BArgs a{B->n,         B->nblocks,     B->ninst,       B->nchunks,     B->slice_ptr, B->col,
           B->block_inst, B->inst_block0, B->chunk_tile0, B->chunk_inst, B->inst_chunk0,
-          nullptr,      0,              0};
+          nullptr,      0,              0,              B->poly_degree > 0 ? 1 : 0};
   if (B->gnn) {
     a.inst_rows = B->gnn->inst_rows;
     a.use_gnn = 1;
@@ -333,6 +334,11 @@ int check_batch(const esr_batch *B) {
         !G->layer_w || !G->layer_b || !G->dec_w)
       return esr::fail(ESR_ERR_ARG, "null GNN array");
     if (G->grid <= 0 || G->stall_window <= 0) return esr::fail(ESR_ERR_ARG, "bad GNN grid or stall window");
+  }
+  if (B->poly_degree != 0) {
+    if (B->poly_degree < 2 || B->poly_degree > 16) return esr::fail(ESR_ERR_ARG, "poly_degree must be 0 or in [2, 16]");
+    if (B->gnn) return esr::fail(ESR_ERR_ARG, "the polynomial and GNN preconditioners exclude each other");
+    if (!B->invdiag || !B->poly_tmp) return esr::fail(ESR_ERR_ARG, "the polynomial preconditioner needs invdiag and poly_tmp");
   }
   return ESR_OK;
 }

@@ -70,9 +70,11 @@ TILED_REORDER = "tiles"
 PIPE_TILE_TARGET = 1900
 PIPE_LIMITS = dict(max_own=2048, max_local=4096)
 # tile kernel: "auto" (pipelined where the layout allows), "blocked",
-# "pipelined" (its shape from the tile size), "pipelined_512", "pipelined_768"
+# "pipelined" (its shape from the tile size), "pipelined_512", "pipelined_768",
+# "pipelined_1024"
 DEFAULT_TILE_KERNEL = "auto"
-_TILE_KERNELS = {"auto": 0, "blocked": 1, "pipelined": 2, "pipelined_512": 3, "pipelined_768": 4}
+_TILE_KERNELS = {"auto": 0, "blocked": 1, "pipelined": 2, "pipelined_512": 3, "pipelined_768": 4,
+                 "pipelined_1024": 5}
 DEFAULT_PRECISION = "exact"  # "exact" (bitwise the reference) or "fast"
 # compile-time check of the fast arithmetic: one step from a random state,
 # max |fused - per-op| per component over max |h|
@@ -463,15 +465,15 @@ class SweEngine:
         return float(getattr(self.m, self._dt_attr))
 
     def tile_kernel_name(self) -> str:
-        """The tile kernel step() runs: 'pipelined_512', 'pipelined_768' or
-    'blocked'."""
+        """The tile kernel step() runs: 'pipelined_512', 'pipelined_768',
+        'pipelined_1024' or 'blocked'."""
         if not self.tiled:
             return ""
         k = _TILE_KERNELS[self.tile_kernel]
         if k in (0, 2):
             auto = int(_lib.lib().esr_swe_tile_kernel(ctypes.byref(self._tiles)))
             k = auto if k == 0 or auto != 1 else 2
-        return {1: "blocked", 2: "pipelined", 3: "pipelined_512", 4: "pipelined_768"}.get(k, "?")
+        return {1: "blocked", 2: "pipelined", 3: "pipelined_512", 4: "pipelined_768", 5: "pipelined_1024"}.get(k, "?")
 
     def touched_bytes_per_step(self) -> int:
         """HBM bytes one step must move in this layout, each array once."""

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define ESR_GB300_ABI_VERSION 10
+#define ESR_GB300_ABI_VERSION 11
 
 /* element types */
 enum {
@@ -357,18 +357,19 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
  *     stages, the next tile's state copied into shared memory (cp.async)
  *     and its records prefetched into L2 while the current tile computes,
  *     cells (tile and halo alike) assigned round-robin and computed in
- *     pairs with packed FP32x2 arithmetic.  Two CTA shapes, by the cells a
- *     thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
- *     n0 <= 2048) and PIPELINED_768 (768 threads x 2, n0 <= 1536); cells
- *     of level <= 3 past those read their records per stage.  PIPELINED is
- *     the 512-thread shape.  Needs nL <= 4096 in every tile and
- *     slot_info == 1.
+ *     pairs with packed FP32x2 arithmetic.  Three CTA shapes, by the cells
+ *     a thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
+ *     n0 <= 2048), PIPELINED_768 (768 threads x 2, n0 <= 1536) and
+ *     PIPELINED_1024 (1024 threads x 2, n0 <= 2048); cells of level <= 3
+ *     past those read their records per stage.  PIPELINED is the 512-thread
+ *     shape.  Needs nL <= 4096 in every tile and slot_info == 1.
  * AUTO picks a pipelined shape when the layout allows it. */
 #define ESR_SWE_TILE_AUTO 0
 #define ESR_SWE_TILE_BLOCKED 1
 #define ESR_SWE_TILE_PIPELINED 2
 #define ESR_SWE_TILE_PIPELINED_512 3
 #define ESR_SWE_TILE_PIPELINED_768 4
+#define ESR_SWE_TILE_PIPELINED_1024 5
 
 /* The kernel AUTO runs for this layout (BLOCKED, PIPELINED_512 or
  * PIPELINED_768), or -1 if the layout is outside the limits.  No reference
@@ -628,6 +629,14 @@ typedef struct {
   const int32_t *inst_chunk0;/* [ninst + 1] first chunk of each instance   */
   const esr_gnn *gnn;        /* NULL: Jacobi (or no) PCG; else flexible CG
                                 with the GNN preconditioner                */
+  /* Polynomial-Jacobi preconditioner (0 = off; needs gnn == NULL):
+   * z = sum_{j<=d} (I - W A)^j W r, the result of d+1 damped Jacobi sweeps
+   * on A z = r from z = 0, with W = invdiag, which then holds the damped
+   * weights omega/diag.  d in [2, 16]; an even d gives an SPD M for any
+   * omega > 0, an odd d needs omega * lambda_max(D^-1 A) < 2. */
+  void *poly_tmp;            /* [2][n] scratch (FP64 or df64), d > 0       */
+  int32_t poly_degree;       /* d: SpMV sweeps per application             */
+  int32_t pad_poly_;
 } esr_batch;
 
 /* Per-instance device scalars. */
@@ -666,7 +675,9 @@ int esr_bcg_init(const esr_batch *B, const double *b64, const void *b, void *x,
                  int32_t maxiter, void *workspace, void *stream);
 
 /* One compaction launch (lists the chunks of running instances) and `k`
- * lockstep iterations of 3 persistent launches each.  Instances that stop
+ * lockstep iterations of 2 (df64) or 3 (FP64) persistent launches each,
+ * plus poly_degree polynomial sweeps and 5 GNN launches where those
+ * preconditioners are on.  Instances that stop
  * inside the call skip their chunks; the host enqueues calls (e.g. as CUDA
  * graphs) and polls esr_bcg_status between them.  q is scratch [n]. */
 int esr_bcg_iterate(const esr_batch *B, void *x, void *r, void *z, void *p,
@@ -674,8 +685,10 @@ int esr_bcg_iterate(const esr_batch *B, void *x, void *r, void *z, void *p,
 
 /* For every converged, unverified instance: x64 = x, r64 = b64 - A64 x64 in
  * FP64; verified = 1 when ||r64|| <= tol.  Otherwise r = r64 replaces the
- * recurrence residual (z = M r, p = z + (r.z / r.z_old) p) and the
- * instance runs again.  4 launches. */
+ * recurrence residual (z = M r, and p = z + (r.z / r.z_old) p while
+ * ||r64|| <= 2 ||r||, else p = z; with the polynomial preconditioner the
+ * next iteration's sweeps form z and beta) and the instance runs again.
+ * 4 launches. */
 int esr_bcg_verify(const esr_batch *B, const double *b64, void *x, double *x64,
                    double *r64, void *r, void *z, void *p, void *workspace,
                    void *stream);

@@ -116,3 +116,60 @@ def test_pack_leaves_out_zero_couplings_but_the_gnn_graph_keeps_them():
     assert stored(lean) == int((s.Ae != 0).sum()) and stored(full) == len(s.Ae)
     x = rng.standard_normal(lean.n)
     assert np.array_equal(_sell_apply(lean, x), _sell_apply(full, x))
+
+
+def test_poly_jacobi_oracle_is_the_neumann_polynomial():
+    """The oracle's polynomial-Jacobi preconditioner (d+1 damped Jacobi
+    sweeps from z = 0) equals sum_{j<=d} (I - W A)^j W r formed densely."""
+    from oracle import cg as ocg
+    n = 7
+    kappa = mesh.kappa_from_field(mesh.gaussian_random_field(n, 3))
+    s = mesh.p1_system(n, kappa)
+    Ae, Av = torch.from_numpy(s.Ae), torch.from_numpy(s.Av)
+    A = lambda v: osp.linsys_apply(v, s.row, s.col, Ae, Av)  # noqa: E731
+    dense = torch.stack([A(e) for e in torch.eye(s.nunk, dtype=torch.float64)], 1)
+    r = torch.from_numpy(np.random.default_rng(1).standard_normal(s.nunk))
+    for d, om in ((2, 0.8), (3, 2 / 3), (4, 0.8)):
+        W = torch.diag(om / Av)
+        T = torch.eye(s.nunk, dtype=torch.float64) - W @ dense
+        ref = sum(torch.linalg.matrix_power(T, j) for j in range(d + 1)) @ W @ r
+        z = ocg.poly_jacobi(A, Av, r, d, om)
+        assert torch.allclose(z, ref, rtol=1e-12, atol=1e-12)
+        # M = p(WA) W is symmetric positive definite on this SPD system
+        M = sum(torch.linalg.matrix_power(T, j) for j in range(d + 1)) @ W
+        assert torch.allclose(M, M.T, rtol=1e-10, atol=1e-12)
+        assert float(torch.linalg.eigvalsh(0.5 * (M + M.T)).min()) > 0.0
+
+
+def test_poly_jacobi_arguments_are_checked_before_any_device_work():
+    import pytest
+    from easier_gb300.numeric.batched import BatchedPCG
+    insts = p1_instances(2, 6, 8, seed=0)
+    for kw, msg in (({"poly_degree": 1}, "poly_degree"), ({"poly_degree": 17}, "poly_degree"),
+                    ({"poly_degree": 4, "jacobi": False}, "jacobi"),
+                    ({"poly_degree": 4, "poly_omega": 0.0}, "poly_omega")):
+        with pytest.raises(ValueError, match=msg):
+            BatchedPCG(insts, device="cuda", **kw)
+
+
+def test_poly_jacobi_batch_rejected_by_the_c_abi():
+    """esr_bcg_init refuses a polynomial batch with a bad degree, a GNN or
+    no scratch before it touches memory (the pointers here are dummies, so
+    the test runs only where no GPU could be reached)."""
+    import ctypes
+    import pytest
+    from easier_gb300 import _lib
+    if torch.cuda.is_available():
+        pytest.skip("dummy device pointers: host-only check")
+    lib = _lib.lib()
+    d = 0x1000
+    g = _lib.Gnn(*([d] * 10), 0.0, 1, 16, 0)
+
+    def batch(degree, tmp=d, gnn=None):
+        return _lib.Batch(256, 1, 1, 256, 1, 1, 1, *([d] * 12), gnn, tmp, degree, 0)
+
+    for b, msg in ((batch(1), b"poly_degree"), (batch(17), b"poly_degree"), (batch(4, tmp=None), b"poly_tmp"),
+                   (batch(4, gnn=ctypes.pointer(g)), b"exclude")):
+        rc = lib.esr_bcg_init(ctypes.byref(b), d, d, d, d, d, d, 1e-8, 0.0, -1, d, None)
+        assert rc == 1, rc  # ESR_ERR_ARG
+        assert msg in lib.esr_last_error()
