@@ -117,6 +117,8 @@ _SIGS = {
     "esr_swe_tile_kernel": (c_int, [POINTER(SweTiles)]),
     "esr_swe_tile_step_with": (c_int, [POINTER(SweTiles), c_int, c_double, _P, _P, c_int64, _P]),
     "esr_bisect_partition": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P]),
+    "esr_bisect_device_workspace_bytes": (c_int64, [c_int64, c_int64, c_int64]),
+    "esr_bisect_partition_device": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P, _P, c_int64, _P]),
     "esr_swe_tile_layout": (c_int, [c_int64, _P, _P, c_int64, _P, POINTER(c_int64), POINTER(c_int64), _P, _P, _P,
                                     _P, _P, _P]),
     "esr_spmv": (c_int, [POINTER(Sell), _P, _P, _P]),

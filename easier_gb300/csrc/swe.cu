@@ -938,52 +938,38 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
                      int64_t nc, int ntiles, float c1, float c3, float c4) {
   using namespace pipe;
   extern __shared__ float smem[];
-  // tile descriptors in shared memory, read where used (registers go to the
-  // face records): three slots, so the one thread 0 fills for the next tile
-  // is never one that a slower warp still reads (the tile before last)
-  __shared__ TileMeta s_meta[3];
-  __shared__ int s_fit[3];
   const Buf SA{smem + 2 * kBuf}, SB{smem + 3 * kBuf};
-  constexpr int kMaxOwnT = TT * CELLS;  // the tile's cells are among the register-held ones
   int t = blockIdx.x;
   if (t >= ntiles) return;
-  if (threadIdx.x == 0) {
-    const TileMeta m0 = tile_meta(meta, off3, offh, t);
-    const bool f = tile_fits(m0, nc, kMaxOwnT);
-    s_meta[0] = m0;
-    s_fit[0] = f;
-    if (!f) esr::raise_status(ESR_DEV_IDX_RANGE);  // outside the kernel's limits: its cells stay unwritten
-  }
-  __syncthreads();
-  int slot = 0, cur = 0;
-  bool fits = s_fit[0] != 0;
+  TileMeta m = tile_meta(meta, off3, offh, t);
+  constexpr int kMaxOwnT = TT * CELLS;  // the tile's cells are among the register-held ones
+  bool fits = tile_fits(m, nc, kMaxOwnT);
+  int cur = 0;
   GeoPair gp[CELLS / 2];
   int hidx[2];
   if (fits) {  // prologue: the first tile's state and geometry
-    const TileMeta &m = s_meta[0];
     halo_index<TT>(m, halo, hidx);
     fetch_own<TT>(Buf{smem}, m, sin);
     fetch_halo<TT>(Buf{smem}, m, sin, nc, halo, hidx);
     load_tile_geo<TT, CELLS>(m, gslot, gp);
+  } else {
+    esr::raise_status(ESR_DEV_IDX_RANGE);
   }
   cp_commit();
   while (true) {
     const int tn = t + gridDim.x;
-    const bool next = tn < ntiles;
-    const int nslot = slot == 2 ? 0 : slot + 1;
-    if (threadIdx.x == 0 && next) {
-      const TileMeta mn = tile_meta(meta, off3, offh, tn);
-      const bool f = tile_fits(mn, nc, kMaxOwnT);
-      s_meta[nslot] = mn;
-      s_fit[nslot] = f;
-      if (!f) esr::raise_status(ESR_DEV_IDX_RANGE);
+    TileMeta mn{};
+    bool next = tn < ntiles;
+    if (next) {
+      mn = tile_meta(meta, off3, offh, tn);
+      if (!tile_fits(mn, nc, kMaxOwnT)) {  // outside the kernel's limits: flag it, leave its cells unwritten
+        esr::raise_status(ESR_DEV_IDX_RANGE);
+      }
     }
     cp_wait_all();
-    __syncthreads();  // this tile's state is in buffer `cur`; the other buffer is free; s_meta[nslot] is set
+    __syncthreads();  // this tile's state is in buffer `cur`; the other buffer is free
     const Buf S0{smem + cur * kBuf}, S0n{smem + (cur ^ 1) * kBuf};
-    const TileMeta &m = s_meta[slot];
-    const TileMeta &mn = s_meta[nslot];
-    const bool nfit = next && s_fit[nslot] != 0;
+    const bool nfit = next && tile_fits(mn, nc, kMaxOwnT);
     if (nfit) {
       if (threadIdx.x == 0) {  // the next tile's face records into L2
         const float4 *g = gslot + 3 * mn.o3;
@@ -1011,23 +997,18 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
     if (!next) break;
     // the next tile's geometry: this thread is done with the current one
     if (nfit) load_tile_geo<TT, CELLS>(mn, gslot, gp);
+    m = mn;
     fits = nfit;
     t = tn;
-    slot = nslot;
     cur ^= 1;
   }
   cp_wait_all();
 }
 
 // CTA shapes of the pipelined kernel: 512 threads x 4 tile cells (what
-// PIPELINED and AUTO run; measured fastest at N=2000 with 1,900-cell tiles),
-// 768 threads x 2 (n0 <= 1536) and 1024 x 2 (on request)
+// PIPELINED and AUTO run; measured fastest at N=2000 with 1,900-cell tiles)
+// and 768 threads x 2 (n0 <= 1536; on request)
 constexpr int kPipeSmall = 768 * 2, kPipeLarge = 512 * 4;
-
-bool pipe_shape_known(int shape) {
-  return shape == ESR_SWE_TILE_PIPELINED_512 || shape == ESR_SWE_TILE_PIPELINED_768 ||
-         shape == ESR_SWE_TILE_PIPELINED_1024;
-}
 
 bool pipe_fits(const esr_swe_tiles *T, int shape) {
   const int max_own = shape == ESR_SWE_TILE_PIPELINED_768 ? kPipeSmall : kPipeLarge;
@@ -1062,8 +1043,6 @@ int run_pipe(const esr_swe_tiles *tiles, int shape, double dt, void *state_a, vo
              cudaStream_t s) {
   if (shape == ESR_SWE_TILE_PIPELINED_768)
     return run_pipe_shape<768, 2>(tiles, dt, state_a, state_b, steps, s);
-  if (shape == ESR_SWE_TILE_PIPELINED_1024)
-    return run_pipe_shape<1024, 2>(tiles, dt, state_a, state_b, steps, s);
   return run_pipe_shape<512, 4>(tiles, dt, state_a, state_b, steps, s);
 }
 
@@ -1130,11 +1109,11 @@ extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, do
   if (((uintptr_t)state_a | (uintptr_t)state_b) % 16) return esr::fail(ESR_ERR_ARG, "state buffers must be 16-byte aligned");
   if (kernel == ESR_SWE_TILE_AUTO) kernel = esr_swe_tile_kernel(tiles);
   if (kernel == ESR_SWE_TILE_PIPELINED) kernel = pipe_shape(tiles);
-  if (pipe_shape_known(kernel)) {
+  if (kernel == ESR_SWE_TILE_PIPELINED_512 || kernel == ESR_SWE_TILE_PIPELINED_768) {
     if (!pipe_fits(tiles, kernel))
       return esr::fail(ESR_ERR_UNSUPPORTED, "the pipelined tile kernel needs fast arithmetic, slot_info == 1, <= 4096 "
-                                            "local cells a tile and <= 2048 own cells (512- and 1024-thread shapes) "
-                                            "or <= 1536 (768-thread)");
+                                            "local cells a tile and <= 2048 own cells (512-thread shape) or <= 1536 "
+                                            "(768-thread)");
   } else if (kernel != ESR_SWE_TILE_BLOCKED) {
     return esr::fail(ESR_ERR_ARG, "unknown tile kernel");
   }

@@ -86,23 +86,33 @@ def _load_selector(sel: _m.Selector, device) -> None:
 
 def _load_reducer(red: _m.Reducer, device) -> None:
     from . import mesh
-    idx = red.easier_data_loader.fully_load("cpu")
+    idx = red.easier_data_loader.fully_load(device if torch.device(device).type == "cuda" else "cpu")
     if idx.dtype not in (torch.int64, torch.int32, torch.int16, torch.int8, torch.uint8):
         raise EasierJitException(f"{red.easier_hint_name}: Reducer idx must be an integer tensor")
     if red.reduce not in ("sum", "prod", "mean", "amax", "amin"):
         raise EasierJitException(f"{red.easier_hint_name}: unknown reduce op {red.reduce!r}")
     if not isinstance(red.n, int) or red.n < 0:
         raise EasierJitException(f"{red.easier_hint_name}: Reducer.n must be a non-negative int")
-    idx_np = idx.to(torch.int64).reshape(-1).numpy()
-    if idx_np.shape[0] >= 2 ** 31 - 1 or red.n >= 2 ** 31 - 1:
+    idx = idx.to(torch.int64).reshape(-1)
+    if idx.shape[0] >= 2 ** 31 - 1 or red.n >= 2 ** 31 - 1:
         raise EasierJitException(f"{red.easier_hint_name}: Reducer larger than int32 indexing")
-    try:
-        rowptr, perm = mesh.csr_from_index(idx_np, red.n)
-    except ValueError as e:
-        raise EasierJitException(f"{red.easier_hint_name}: {e}") from e
-    red.idx = torch.from_numpy(idx_np).to(device)
-    red._rowptr32 = torch.from_numpy(rowptr.astype(np.int32)).to(device)
-    red._perm32 = torch.from_numpy(perm.astype(np.int32)).to(device)
+    if torch.device(device).type == "cuda":
+        # the stable CSR on the GPU: one stable sort, the same arrays as
+        # esr_csr_from_index
+        idx = idx.to(device)
+        if idx.numel() and (int(idx.min()) < 0 or int(idx.max()) >= red.n):
+            raise EasierJitException(f"{red.easier_hint_name}: Reducer index out of range [0, {red.n})")
+        red.idx = idx
+        red._rowptr32, red._perm32 = mesh._stable_csr_device(idx, red.n)
+    else:
+        idx_np = idx.numpy()
+        try:
+            rowptr, perm = mesh.csr_from_index(idx_np, red.n)
+        except ValueError as e:
+            raise EasierJitException(f"{red.easier_hint_name}: {e}") from e
+        red.idx = torch.from_numpy(idx_np).to(device)
+        red._rowptr32 = torch.from_numpy(rowptr.astype(np.int32)).to(device)
+        red._perm32 = torch.from_numpy(perm.astype(np.int32)).to(device)
     red.easier_index_status = "rewritten"
     red.set_is_full()
 

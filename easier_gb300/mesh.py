@@ -283,11 +283,31 @@ def sell_layout(n: int, rowptr: np.ndarray, perm: np.ndarray, colidx: np.ndarray
     return slice_ptr, col, src_pos
 
 
-def bisect_partition(n: int, src: np.ndarray, dst: np.ndarray, max_part: int):
-    """Recursive-BFS-bisection parts of at most max_part vertices."""
+def bisect_partition(n: int, src, dst, max_part: int):
+    """Recursive-BFS-bisection parts of at most max_part vertices.  CUDA
+    tensors: on the GPU (esr_bisect_partition_device), returning a CUDA
+    int64 tensor; else on the host, returning a numpy array."""
+    if isinstance(src, torch.Tensor) and src.is_cuda:
+        return _bisect_partition_device(n, src, dst, max_part)
     src, dst = _i64(src), _i64(dst)
     part = np.empty(n, np.int64)
     nparts = ctypes.c_int64()
     _lib.call("esr_bisect_partition", n, src.shape[0], _lib.ptr(src), _lib.ptr(dst), int(max_part), _lib.ptr(part),
               ctypes.byref(nparts))
     return part, int(nparts.value)
+
+
+def _bisect_partition_device(n: int, src: torch.Tensor, dst: torch.Tensor, max_part: int):
+    dev = src.device
+    src = src.to(torch.int64).contiguous()
+    dst = dst.to(dev, torch.int64).contiguous()
+    m = src.shape[0]
+    nbytes = int(_lib.lib().esr_bisect_device_workspace_bytes(n, m, int(max_part)))
+    if nbytes < 0:
+        raise ValueError("graph sizes out of range for the device partition")
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    part = torch.empty(n, dtype=torch.int32, device=dev)
+    nparts = ctypes.c_int64()
+    _lib.call("esr_bisect_partition_device", n, m, _lib.ptr(src), _lib.ptr(dst), int(max_part), _lib.ptr(part),
+              ctypes.byref(nparts), _lib.ptr(ws), nbytes, _lib.stream_handle(dev))
+    return part.to(torch.int64), int(nparts.value)

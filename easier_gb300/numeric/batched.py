@@ -20,6 +20,7 @@ A single system is a batch of one (``CG.solve(precision="df64")``).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
@@ -200,6 +201,7 @@ class BatchedPCG:
             raise ValueError("BatchedPCG runs on a CUDA device")
         if gnn is not None and not jacobi:
             raise ValueError("the GNN preconditioner falls back to Jacobi: jacobi must be True")
+        _drain_pending()
         poly_degree = int(poly_degree)
         if poly_degree:
             if not 2 <= poly_degree <= 16:
@@ -475,20 +477,20 @@ class BatchedPCG:
 
     def _free_graphs(self):
         graphs = getattr(self, "_one_graphs", {})
-        if graphs:
-            try:  # no launch of them may still be running
-                torch.cuda.current_stream(self.dev).synchronize()
-            except Exception:  # interpreter shutdown
-                pass
-        for h in graphs.values():
-            try:
-                _lib.call("esr_bcg_graph_destroy", h)
-            except Exception:  # interpreter shutdown
-                pass
         self._one_graphs = {}
+        if graphs:
+            _destroy_graphs(list(graphs.values()), self.dev)
+        _drain_pending()
 
     def __del__(self):
-        self._free_graphs()
+        # the collector can run this while some stream is being captured
+        # into a CUDA graph, where a synchronisation or a graph teardown
+        # would invalidate that capture: the handles wait for a safe point
+        # (the next engine call that frees graphs, or interpreter exit)
+        graphs, captured = getattr(self, "_one_graphs", {}), getattr(self, "_graphs", {})
+        if graphs or captured:  # (the torch graphs are released there too)
+            _PENDING_GRAPHS.append((list(graphs.values()), getattr(self, "dev", None), list(captured.values())))
+            self._one_graphs, self._graphs = {}, {}
 
     def solve(self, rtol: float = 1e-8, atol: Optional[float] = None, maxiter: Optional[int] = None,
               max_rounds: int = 16) -> List[dict]:
@@ -517,6 +519,29 @@ class BatchedPCG:
 
 
 _TUNE_CACHE: dict = {}
+_PENDING_GRAPHS: list = []  # (graph handles, device, torch graphs) of collected engines
+
+
+def _destroy_graphs(handles, dev) -> None:
+    try:  # no launch of them may still be running
+        torch.cuda.synchronize(dev)
+    except Exception:  # interpreter shutdown
+        pass
+    for h in handles:
+        try:
+            _lib.call("esr_bcg_graph_destroy", h)
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def _drain_pending() -> None:
+    while _PENDING_GRAPHS:
+        handles, dev, captured = _PENDING_GRAPHS.pop()
+        _destroy_graphs(handles, dev)
+        del captured
+
+
+atexit.register(_drain_pending)
 
 
 def p1_sides(count: int, nmin: int, nmax: int, seed: int = 0) -> np.ndarray:

@@ -65,16 +65,18 @@ DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
 # tile-major: the partition alone, without the RCM pass).  Measured at
 # N=2000: the same kernel time (0.454 vs 0.457 ms), 2 s less compile.
 TILED_REORDER = "tiles"
+# build the tiled layout of a CUDA engine on the GPU (esr_bisect_partition_device
+# and torch sorts); False: the host functions (same arrays for the same
+# partition; the host partition itself differs, see esr_bisect_partition_device)
+LAYOUT_ON_DEVICE = True
 # Fast arithmetic on large meshes: tiles for the pipelined tile kernel
 # (<= 2048 own cells, <= 4096 local cells)
 PIPE_TILE_TARGET = 1900
 PIPE_LIMITS = dict(max_own=2048, max_local=4096)
 # tile kernel: "auto" (pipelined where the layout allows), "blocked",
-# "pipelined" (its shape from the tile size), "pipelined_512", "pipelined_768",
-# "pipelined_1024"
+# "pipelined" (its shape from the tile size), "pipelined_512", "pipelined_768"
 DEFAULT_TILE_KERNEL = "auto"
-_TILE_KERNELS = {"auto": 0, "blocked": 1, "pipelined": 2, "pipelined_512": 3, "pipelined_768": 4,
-                 "pipelined_1024": 5}
+_TILE_KERNELS = {"auto": 0, "blocked": 1, "pipelined": 2, "pipelined_512": 3, "pipelined_768": 4}
 DEFAULT_PRECISION = "exact"  # "exact" (bitwise the reference) or "fast"
 # compile-time check of the fast arithmetic: one step from a random state,
 # max |fused - per-op| per component over max |h|
@@ -261,9 +263,8 @@ class SweEngine:
     def _build_layout(self) -> None:
         b = self.b
         nc = b["nc"]
-        src = b["selectors"]["gather_src"].idx.cpu().numpy().astype(np.int64)
-        dst = b["selectors"]["gather_dst"].idx.cpu().numpy().astype(np.int64)
-        bcell = b["selectors"]["gather_b"].idx.cpu().numpy().astype(np.int64)
+        sel = b["selectors"]
+        idx = [sel[k].idx for k in ("gather_src", "gather_dst", "gather_b")]
         want_tiles = self.mode in ("tiled", "auto") and self.dtype == torch.float32
         tiles = None
         tile_cells = self.tile_cells
@@ -271,11 +272,26 @@ class SweEngine:
         while True:
             reorder = TILED_REORDER if (want_tiles and self.reorder == "rcm") else self.reorder
             self.layout_order = reorder if want_tiles else self.reorder
+            # the tiled layout of a CUDA engine is built on the GPU (partition,
+            # slots, rings); RCM numberings are a host pass
+            on_gpu = self.device.type == "cuda" and reorder != "rcm" and LAYOUT_ON_DEVICE
+            src, dst, bcell = ([a.to(self.device, torch.int64) for a in idx] if on_gpu else
+                               [a.cpu().numpy().astype(np.int64) for a in idx])
             lay = cell_layout(nc, src, dst, bcell, reorder=reorder,
                               tile_cells=tile_cells if want_tiles else None)
             if lay["part"] is None:
                 break
             tiles = tile_layout(lay["nbr"], lay["part"])
+            if self.precision == "fast" and reorder != "rcm":
+                # a few over-wide tiles: cut them rather than shrink every tile
+                for _ in range(2):
+                    if tiles["stats"]["max_own"] > PIPE_LIMITS["max_own"]:
+                        break
+                    split = split_wide_tiles(lay, tiles, PIPE_LIMITS["max_local"])
+                    if split is None:
+                        break
+                    lay = cell_layout(nc, src, dst, bcell, reorder=reorder, part=split)
+                    tiles = tile_layout(lay["nbr"], lay["part"])
             st = tiles["stats"]
             if st["max_own"] <= TILE_CELLS and st["max_l3"] <= TILE_MAX_L3 and st["smem"] <= TILE_SMEM:
                 # fast arithmetic: smaller tiles until the pipelined kernel takes them
@@ -291,14 +307,12 @@ class SweEngine:
                 continue
             want_tiles = False
         self.tile_cells = tile_cells
-        order, nbr, pos, width, part = lay["order"], lay["nbr"], lay["pos"], lay["width"], lay["part"]
+        order, nbr, pos, width = lay["order"], lay["nbr"], lay["pos"], lay["width"]
         tiled = tiles is not None
-        self.order_np = order
-        self.order = torch.from_numpy(order).to(self.device)
+        self.order = _to(order, self.device)
         self.width = width
-        self.nbr_np = nbr
-        self.nbr = torch.from_numpy(nbr).to(self.device)
-        self.slot_pos = torch.from_numpy(pos).to(self.device)
+        self.nbr = _to(nbr, self.device)
+        self.slot_pos = _to(pos, self.device)
         self.tiled = tiled
         if tiled:
             self._build_tiles(tiles)
@@ -312,15 +326,15 @@ class SweEngine:
     def _build_tiles(self, lay: dict) -> None:
         st = lay["stats"]
         dev = self.device
-        self.tile_meta = torch.from_numpy(lay["meta"].reshape(-1)).to(dev)
-        self.tile_off3 = torch.from_numpy(lay["off3"]).to(dev)
-        self.tile_offh = torch.from_numpy(lay["offh"]).to(dev)
-        halo = lay["halo"]
-        self.tile_halo = torch.from_numpy(halo if halo.size else np.zeros(1, np.int32)).to(dev)
-        self.tile_lnbr = torch.from_numpy(lay["lnbr"]).to(dev)
-        self.tile_gsrc = torch.from_numpy(lay["slot_src"]).to(dev)
-        self.tile_area_src = torch.from_numpy(lay["area_src"]).to(dev)
-        self.tile_fast_order = torch.from_numpy(_slots_by_neighbour(lay["meta"], lay["off3"], lay["lnbr"])).to(dev)
+        self.tile_meta = _to(lay["meta"], dev).reshape(-1).contiguous()
+        self.tile_off3 = _to(lay["off3"], dev)
+        self.tile_offh = _to(lay["offh"], dev)
+        halo = _to(lay["halo"], dev)
+        self.tile_halo = halo if halo.numel() else torch.zeros(1, dtype=torch.int32, device=dev)
+        self.tile_lnbr = _to(lay["lnbr"], dev)
+        self.tile_gsrc = _to(lay["slot_src"], dev)
+        self.tile_area_src = _to(lay["area_src"], dev)
+        self.tile_fast_order = _to(_slots_by_neighbour(lay["meta"], lay["off3"], lay["lnbr"]), dev)
         self.ntiles = st["ntiles"]
         self.tile_stats = st
 
@@ -465,15 +479,15 @@ class SweEngine:
         return float(getattr(self.m, self._dt_attr))
 
     def tile_kernel_name(self) -> str:
-        """The tile kernel step() runs: 'pipelined_512', 'pipelined_768',
-        'pipelined_1024' or 'blocked'."""
+        """The tile kernel step() runs: 'pipelined_512', 'pipelined_768' or
+        'blocked'."""
         if not self.tiled:
             return ""
         k = _TILE_KERNELS[self.tile_kernel]
         if k in (0, 2):
             auto = int(_lib.lib().esr_swe_tile_kernel(ctypes.byref(self._tiles)))
             k = auto if k == 0 or auto != 1 else 2
-        return {1: "blocked", 2: "pipelined", 3: "pipelined_512", 4: "pipelined_768", 5: "pipelined_1024"}.get(k, "?")
+        return {1: "blocked", 2: "pipelined", 3: "pipelined_512", 4: "pipelined_768"}.get(k, "?")
 
     def touched_bytes_per_step(self) -> int:
         """HBM bytes one step must move in this layout, each array once."""
@@ -508,6 +522,10 @@ class SweEngine:
         return f"swe_tiled_{self.tile_kernel_name()}_{self.precision}"
 
 
+def _to(a, dev) -> torch.Tensor:
+    return a.to(dev) if isinstance(a, torch.Tensor) else torch.from_numpy(a).to(dev)
+
+
 def slot_width(nc: int, nd: np.ndarray, nb: np.ndarray) -> int:
     total = np.bincount(nd, minlength=nc) + np.bincount(nb, minlength=nc)
     wmax = int(total.max()) if total.size else 0
@@ -517,7 +535,7 @@ def slot_width(nc: int, nd: np.ndarray, nb: np.ndarray) -> int:
 
 
 def cell_layout(nc: int, src: np.ndarray, dst: np.ndarray, bcell: np.ndarray, reorder: str = "rcm",
-                tile_cells: Optional[int] = None) -> dict:
+                tile_cells: Optional[int] = None, part=None) -> dict:
     """Cell numbering and face slots of the fused step.
 
     order[new] = original cell.  RCM numbering, or (tile_cells given and 3
@@ -525,19 +543,28 @@ def cell_layout(nc: int, src: np.ndarray, dst: np.ndarray, bcell: np.ndarray, re
     tiles from recursive BFS bisection.  nbr [width, nc]: neighbour (new
     numbering), -1 wall, -2 empty; slots hold a cell's in-edges in the
     reference's edge order, then its wall faces.  pos [width, nc]: source of
-    each slot's values (edge e -> e, wall face b -> ne + b, none -> -1)."""
+    each slot's values (edge e -> e, wall face b -> ne + b, none -> -1).
+    ``part`` (reorder 'tiles' or 'none'): the tile of every cell, instead of
+    the bisection."""
+    if isinstance(src, torch.Tensor) and src.is_cuda:
+        return _cell_layout_device(nc, src, dst, bcell, reorder, tile_cells, part)
+    if part is not None and reorder == "rcm":
+        raise ValueError("a given partition needs the module's own numbering")
     ne, nbc = src.shape[0], bcell.shape[0]
     order = mesh.rcm_order(nc, src, dst) if (reorder == "rcm" and nc > 1) else np.arange(nc, dtype=np.int64)
     inv = np.empty(nc, np.int64)
     inv[order] = np.arange(nc, dtype=np.int64)
     width = slot_width(nc, inv[dst], inv[bcell])
-    part = None
-    if tile_cells is not None and width == 3 and nc > 0:
-        part, _ = mesh.bisect_partition(nc, inv[src], inv[dst], tile_cells)
+    if (tile_cells is not None or part is not None) and width == 3 and nc > 0:
+        if part is None:
+            part, _ = mesh.bisect_partition(nc, inv[src], inv[dst], tile_cells)
+        part = np.asarray(part, dtype=np.int64)
         tmajor = np.argsort(part, kind="stable")
         order = order[tmajor]
         part = part[tmajor]
         inv[order] = np.arange(nc, dtype=np.int64)
+    else:
+        part = None
     nd = inv[dst]
     rowptr, perm = mesh.csr_from_index(nd, nc)
     nb = inv[bcell]
@@ -556,22 +583,227 @@ def cell_layout(nc: int, src: np.ndarray, dst: np.ndarray, bcell: np.ndarray, re
     return dict(order=order, nbr=nbr, pos=pos, width=width, part=part)
 
 
+def _cell_layout_device(nc: int, src: torch.Tensor, dst: torch.Tensor, bcell: torch.Tensor, reorder: str,
+                        tile_cells: Optional[int], part=None) -> dict:
+    """cell_layout on the GPU (CUDA tensors in and out) for the module's own
+    numbering ('tiles' or 'none'; RCM is a host pass): the partition from
+    esr_bisect_partition_device, the rest the same torch operations as the
+    numpy ones (a stable sort is the stable CSR of esr_csr_from_index)."""
+    if reorder == "rcm":
+        raise ValueError("the device cell layout keeps the module's numbering ('tiles' or 'none')")
+    dev = src.device
+    src, dst, bcell = (a.to(dev, torch.int64) for a in (src, dst, bcell))
+    ne, nbc = src.shape[0], bcell.shape[0]
+    ar = torch.arange(nc, dtype=torch.int64, device=dev)
+    order, inv = ar, ar
+    total = torch.bincount(dst, minlength=nc) + torch.bincount(bcell, minlength=nc)
+    wmax = int(total.max()) if nc else 0
+    if wmax > 4:
+        raise NotImplementedError(f"a cell has {wmax} faces; the fused kernels handle at most 4")
+    width = 3 if wmax <= 3 else 4
+    if (tile_cells is not None or part is not None) and width == 3 and nc > 0:
+        if part is None:
+            part, _ = mesh.bisect_partition(nc, src, dst, tile_cells)
+        part = torch.as_tensor(part, device=dev).to(torch.int64)
+        order = torch.sort(part, stable=True).indices
+        part = part[order]
+        inv = torch.empty_like(order)
+        inv[order] = ar
+    else:
+        part = None
+    nd, nb = inv[dst], inv[bcell]
+    rowptr, perm = mesh._stable_csr_device(nd, nc)
+    browptr, bperm = mesh._stable_csr_device(nb, nc)
+    rowptr, perm, browptr, bperm = (a.to(torch.int64) for a in (rowptr, perm, browptr, bperm))
+    deg = rowptr[1:] - rowptr[:-1]
+    cell_of_edge = nd[perm]
+    k_edge = torch.arange(ne, dtype=torch.int64, device=dev) - rowptr[cell_of_edge]
+    cell_of_wall = nb[bperm]
+    k_wall = deg[cell_of_wall] + (torch.arange(nbc, dtype=torch.int64, device=dev) - browptr[cell_of_wall])
+    nbr = torch.full((width, nc), -2, dtype=torch.int32, device=dev)
+    nbr[k_edge, cell_of_edge] = inv[src[perm]].to(torch.int32)
+    nbr[k_wall, cell_of_wall] = -1
+    pos = torch.full((width, nc), -1, dtype=torch.int64, device=dev)
+    pos[k_edge, cell_of_edge] = perm
+    pos[k_wall, cell_of_wall] = ne + bperm
+    return dict(order=order, nbr=nbr, pos=pos, width=width, part=part)
+
+
+def split_wide_tiles(lay: dict, tiles: dict, limit: int):
+    """The partition (in the module's numbering) of `lay` with every tile
+    whose local list (tile and four rings) exceeds `limit` cells cut in two
+    by a BFS bisection of its own cells (the halves become new tiles after
+    the others); None when no tile exceeds it.  A long, thin tile -- which a
+    bisection cut along an irregular BFS level can leave -- has a halo near
+    its own size; its halves have about half of it each."""
+    meta = tiles["meta"]
+    nl = np.asarray(meta[:, 5].cpu() if isinstance(meta, torch.Tensor) else meta[:, 5]).astype(np.int64)
+    wide = np.nonzero(nl > limit)[0]
+    if wide.size == 0:
+        return None
+    meta_np = np.asarray(meta.cpu() if isinstance(meta, torch.Tensor) else meta)
+    part = lay["part"]
+    dev = part.device if isinstance(part, torch.Tensor) else None
+    new = part.cpu().numpy().copy() if dev is not None else np.asarray(part).copy()
+    nbr = lay["nbr"]
+    next_id = int(meta_np.shape[0])
+    for t in wide:
+        b, n0 = int(meta_np[t, 0]), int(meta_np[t, 1])
+        sub = nbr[:, b:b + n0]
+        sub = sub.cpu().numpy() if isinstance(sub, torch.Tensor) else np.asarray(sub)
+        c = np.broadcast_to(np.arange(n0, dtype=np.int64), sub.shape)
+        inside = (sub >= b) & (sub < b + n0)
+        half, _ = mesh.bisect_partition(n0, c[inside], sub[inside].astype(np.int64) - b, (n0 + 1) // 2)
+        new[b + np.nonzero(half == 1)[0]] = next_id
+        next_id += 1
+    order = lay["order"]
+    order = order.cpu().numpy() if isinstance(order, torch.Tensor) else np.asarray(order)
+    out = np.empty_like(new)
+    out[order] = new
+    return torch.from_numpy(out).to(dev) if dev is not None else out
+
+
+def _isin_sorted(keys: torch.Tensor, sorted_keys: torch.Tensor) -> torch.Tensor:
+    if sorted_keys.numel() == 0:
+        return torch.zeros(keys.shape, dtype=torch.bool, device=keys.device)
+    p = torch.searchsorted(sorted_keys, keys).clamp_(max=sorted_keys.numel() - 1)
+    return sorted_keys[p] == keys
+
+
+def _tile_layout_device(nbr: torch.Tensor, part: torch.Tensor) -> dict:
+    """esr_swe_tile_layout on the GPU, the same arrays (as CUDA tensors).
+    Ring L of a tile is the set of (tile, cell) keys reached from ring L-1
+    through a face slot, minus the tile's own cells and rings L-1 and L-2
+    (a neighbour is at most one ring away), deduplicated and sorted by one
+    torch.unique; positions in the local lists come from sorted-key
+    searches."""
+    dev = nbr.device
+    nbr = nbr.to(torch.int32).contiguous()
+    nc = nbr.shape[1]
+    if nc == 0:
+        raise ValueError("empty layout")
+    part = part.to(dev, torch.int64).contiguous()
+    if int(part.min()) < 0 or bool((part[1:] < part[:-1]).any()):
+        raise ValueError("part must be non-decreasing tile ids")
+    if bool(((nbr < -2) | (nbr >= nc)).any()):
+        raise ValueError("face slot out of range")
+    ntiles = int(part[-1]) + 1
+    i64 = dict(dtype=torch.int64, device=dev)
+    n0 = torch.bincount(part, minlength=ntiles)
+    if bool((n0 == 0).any()):
+        raise ValueError("tile ids skip a value")
+    tbeg = torch.cumsum(n0, 0) - n0
+    g64 = nbr.to(torch.int64)
+    K = nc  # key of (tile t, cell g): t * nc + g
+
+    def ring(cells, tiles, exclude):
+        g = g64[:, cells]
+        t = tiles.unsqueeze(0).expand(3, -1)
+        gs = g.clamp(min=0)
+        keep = (g >= 0) & (part[gs] != t)
+        keys = t * K + gs
+        for ex in exclude:
+            keep &= ~_isin_sorted(keys, ex)
+        return torch.unique(keys[keep])
+
+    rings = [ring(torch.arange(nc, **i64), part, [])]
+    for _ in range(3):
+        r = rings[-1]
+        rings.append(ring(r % K, r // K, rings[-1:] + rings[-2:-1]))
+    counts = [torch.bincount(r // K, minlength=ntiles) for r in rings]
+    cum = [n0]
+    for c in counts:
+        cum.append(cum[-1] + c)
+    meta = torch.zeros((ntiles, 8), dtype=torch.int32, device=dev)
+    meta[:, 0] = tbeg.to(torch.int32)
+    for q in range(5):
+        meta[:, 1 + q] = cum[q].to(torch.int32)
+    n3, nL = cum[3], cum[4]
+    nh = nL - n0
+    off3 = torch.cumsum(n3, 0) - n3
+    offh = torch.cumsum(nh, 0) - nh
+    tot3, toth = int(n3.sum()), int(nh.sum())
+    # halo: each tile's rings 1..4 in order, each ascending; the local index
+    # of ring L's i-th entry of tile t is cum[L-1][t] + (i - first entry of t)
+    halo = torch.zeros(toth + 1, dtype=torch.int64, device=dev)  # + 1: a safe index for tiles without halo
+    keys, local = [], []
+    for L, (r, c) in enumerate(zip(rings, counts), start=1):
+        t = r // K
+        first = torch.cumsum(c, 0) - c
+        li = cum[L - 1][t] + (torch.arange(r.numel(), **i64) - first[t])
+        halo[offh[t] + (li - n0[t])] = r % K
+        keys.append(r)
+        local.append(li)
+    keys, srt = torch.sort(torch.cat(keys))
+    local = torch.cat(local)[srt]
+    # the face slots of every tile's cells of level <= 3
+    tile = torch.repeat_interleave(torch.arange(ntiles, **i64), n3)
+    j = torch.arange(tot3, **i64) - off3[tile]
+    n0t = n0[tile]
+    cell = torch.where(j < n0t, tbeg[tile] + j, halo[offh[tile] + (j - n0t).clamp(min=0)])
+    lnbr = torch.empty(3 * tot3, dtype=torch.int32, device=dev)
+    slot_src = torch.empty(3 * tot3, **i64)
+    for k in range(3):
+        g = g64[k, cell]
+        gs = g.clamp(min=0)
+        own = part[gs] == tile
+        key = tile * K + gs
+        p = torch.searchsorted(keys, key).clamp_(max=max(keys.numel() - 1, 0))
+        hl = local[p] if keys.numel() else torch.zeros_like(key)
+        lp = torch.where(g < 0, g, torch.where(own, gs - tbeg[tile], hl))
+        if bool(((g >= 0) & ~own & ((keys[p] != key) if keys.numel() else True)).any()):
+            raise RuntimeError("tile layout: a neighbour of a level-3 cell is outside the local list")
+        d = 3 * off3[tile] + k * n3[tile] + j
+        lnbr[d] = lp.to(torch.int32)
+        slot_src[d] = k * nc + cell
+    halo = halo[:toth].to(torch.int32)
+    max_own, max_l3, max_local = int(n0.max()), int(n3.max()), int(nL.max())
+    stats = dict(ntiles=ntiles, max_own=max_own, max_l3=max_l3, max_local=max_local,
+                 max_halo3=int((n3 - n0).max()), slot_info=int(_one_boundary_slot(meta, lnbr)),
+                 mean_own=float(n0.double().mean()), l3_over_own=float(tot3 / nc),
+                 local_over_own=float(int(nL.sum()) / nc), smem=(3 * max_local + 6 * max_l3) * 4)
+    return dict(meta=meta, off3=off3, offh=offh, halo=halo, lnbr=lnbr, slot_src=slot_src, area_src=cell,
+                stats=stats)
+
+
+def _local_slots(meta, off3):
+    """[3, total] positions 3 * off3[t] + k * n3[t] + j of the records of
+    every tile's cells of level <= 3 (torch or numpy, as given)."""
+    if isinstance(meta, torch.Tensor):
+        dev = meta.device
+        n3 = meta[:, 4].to(torch.int64)
+        total = int(n3.sum())
+        tile = torch.repeat_interleave(torch.arange(n3.shape[0], device=dev), n3)
+        j = torch.arange(total, device=dev) - torch.repeat_interleave(torch.cumsum(n3, 0) - n3, n3)
+        o3 = off3.to(dev, torch.int64) if off3 is not None else (torch.cumsum(n3, 0) - n3)
+        return 3 * o3[tile] + torch.arange(3, device=dev)[:, None] * n3[tile] + j
+    n3 = meta[:, 4].astype(np.int64)
+    total = int(n3.sum())
+    tile = np.repeat(np.arange(n3.shape[0], dtype=np.int64), n3)
+    j = np.arange(total, dtype=np.int64) - np.repeat(np.cumsum(n3) - n3, n3)
+    o3 = off3.astype(np.int64) if off3 is not None else np.concatenate([[0], np.cumsum(n3)[:-1]])
+    return 3 * o3[tile] + np.arange(3, dtype=np.int64)[:, None] * n3[tile] + j
+
+
 def _slots_by_neighbour(meta: np.ndarray, off3: np.ndarray, lnbr: np.ndarray) -> np.ndarray:
     """Record order of the fast-arithmetic tile layout: each cell's three
     face records sorted by local neighbour index (walls and empty slots
     first).  Neighbouring lanes of a warp then read neighbour states at more
     regular offsets: fewer shared-memory bank conflicts (modelled on the
     N=400 mesh: 4.1 -> 3.2 wavefronts per (h, uh) load of a warp)."""
-    order = np.arange(lnbr.shape[0], dtype=np.int64)
-    n3 = meta[:, 4].astype(np.int64)
-    total = int(n3.sum())
-    if total == 0:
+    if isinstance(lnbr, torch.Tensor):
+        order = torch.arange(lnbr.shape[0], dtype=torch.int64, device=lnbr.device)
+        if lnbr.shape[0] == 0:
+            return order
+        idx = _local_slots(meta, off3)
+        k = torch.sort(lnbr[idx].to(torch.int64), dim=0, stable=True).indices
+        order[idx] = torch.gather(idx, 0, k)
         return order
-    # every level-<=3 cell of every tile: its tile and local index j
-    tile = np.repeat(np.arange(n3.shape[0], dtype=np.int64), n3)
-    j = np.arange(total, dtype=np.int64) - np.repeat(np.cumsum(n3) - n3, n3)
-    # its three records: 3 * off3[t] + k * n3[t] + j
-    idx = 3 * off3.astype(np.int64)[tile] + np.arange(3, dtype=np.int64)[:, None] * n3[tile] + j
+    order = np.arange(lnbr.shape[0], dtype=np.int64)
+    if lnbr.shape[0] == 0:
+        return order
+    # every level-<=3 cell of every tile: its three records
+    idx = _local_slots(meta, off3)
     k = np.argsort(lnbr[idx], axis=0, kind="stable")
     order[idx] = np.take_along_axis(idx, k, axis=0)
     return order
@@ -581,15 +813,10 @@ def _one_boundary_slot(meta: np.ndarray, lnbr: np.ndarray) -> bool:
     """True when no tile cell has more than one wall or empty face slot, so
     in the fast layout (records sorted by neighbour, negatives first) slots
     1 and 2 of every cell are interior faces."""
-    n3 = meta[:, 4].astype(np.int64)
-    total = int(n3.sum())
-    if total == 0:
+    if lnbr.shape[0] == 0:
         return True
-    tile = np.repeat(np.arange(n3.shape[0], dtype=np.int64), n3)
-    j = np.arange(total, dtype=np.int64) - np.repeat(np.cumsum(n3) - n3, n3)
-    off3 = np.concatenate([[0], np.cumsum(n3)[:-1]])
-    idx = 3 * off3[tile] + np.arange(3, dtype=np.int64)[:, None] * n3[tile] + j
-    return bool(((lnbr[idx] < 0).sum(axis=0) <= 1).all())
+    idx = _local_slots(meta, None)
+    return bool(((lnbr[idx] < 0).sum(0) <= 1).all())
 
 
 def tile_layout(nbr: np.ndarray, part: np.ndarray) -> dict:
@@ -602,6 +829,8 @@ def tile_layout(nbr: np.ndarray, part: np.ndarray) -> dict:
     levels <= 3 get local face slots.  Returns numpy arrays: meta [ntiles, 8]
     (cell_off, n0, n1, n2, n3, nL), off3, offh, halo, lnbr, slot_src (index
     into the flattened [3, nc] slot arrays), area_src, and stats."""
+    if isinstance(nbr, torch.Tensor) and nbr.is_cuda:
+        return _tile_layout_device(nbr, part)
     nc = nbr.shape[1]
     nbr = np.ascontiguousarray(nbr, dtype=np.int32)
     part = np.ascontiguousarray(part, dtype=np.int64)
@@ -644,10 +873,10 @@ def _verify(m, eng: SweEngine, binding: dict) -> bool:
     the same random state; bitwise equality required."""
     t = binding["tensors"]
     nc, dtype, dev = binding["nc"], binding["dtype"], eng.device
-    g = torch.Generator(device="cpu").manual_seed(1234)
-    h0 = (1.0 + 0.05 * torch.rand(nc, generator=g, dtype=torch.float64)).to(dtype).to(dev)
-    u0 = (0.01 * torch.randn(nc, generator=g, dtype=torch.float64)).to(dtype).to(dev)
-    v0 = (0.01 * torch.randn(nc, generator=g, dtype=torch.float64)).to(dtype).to(dev)
+    g = torch.Generator(device=dev).manual_seed(1234)  # seeded, drawn where the state lives
+    h0 = (1.0 + 0.05 * torch.rand(nc, generator=g, dtype=torch.float64, device=dev)).to(dtype)
+    u0 = (0.01 * torch.randn(nc, generator=g, dtype=torch.float64, device=dev)).to(dtype)
+    v0 = (0.01 * torch.randn(nc, generator=g, dtype=torch.float64, device=dev)).to(dtype)
     saved = {k: (t[k].data, t[k].elempart) for k in ("h", "uh", "vh", "area")}
     state_saved = eng.state.clone()
     cur_saved = eng.cur

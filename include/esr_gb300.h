@@ -357,19 +357,18 @@ int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a,
  *     stages, the next tile's state copied into shared memory (cp.async)
  *     and its records prefetched into L2 while the current tile computes,
  *     cells (tile and halo alike) assigned round-robin and computed in
- *     pairs with packed FP32x2 arithmetic.  Three CTA shapes, by the cells
- *     a thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
- *     n0 <= 2048), PIPELINED_768 (768 threads x 2, n0 <= 1536) and
- *     PIPELINED_1024 (1024 threads x 2, n0 <= 2048); cells of level <= 3
- *     past those read their records per stage.  PIPELINED is the 512-thread
- *     shape.  Needs nL <= 4096 in every tile and slot_info == 1.
+ *     pairs with packed FP32x2 arithmetic.  Two CTA shapes, by the cells a
+ *     thread keeps in registers: PIPELINED_512 (512 threads x 4 cells,
+ *     n0 <= 2048) and PIPELINED_768 (768 threads x 2, n0 <= 1536); cells
+ *     of level <= 3 past those read their records per stage.  PIPELINED is
+ *     the 512-thread shape.  Needs nL <= 4096 in every tile and
+ *     slot_info == 1.
  * AUTO picks a pipelined shape when the layout allows it. */
 #define ESR_SWE_TILE_AUTO 0
 #define ESR_SWE_TILE_BLOCKED 1
 #define ESR_SWE_TILE_PIPELINED 2
 #define ESR_SWE_TILE_PIPELINED_512 3
 #define ESR_SWE_TILE_PIPELINED_768 4
-#define ESR_SWE_TILE_PIPELINED_1024 5
 
 /* The kernel AUTO runs for this layout (BLOCKED, PIPELINED_512 or
  * PIPELINED_768), or -1 if the layout is outside the limits.  No reference
@@ -390,6 +389,21 @@ int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, double dt,
 int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src,
                          const int64_t *dst, int64_t max_part, int64_t *part,
                          int64_t *nparts);
+
+/* Device: the same partition contract on the GPU (src, dst, part device
+ * arrays; n and 2m below 2^31).  The same part sizes in the same order as
+ * esr_bisect_partition; the parts themselves are cut from BFS distances
+ * with ties broken by vertex id, so they are deterministic but not the host
+ * function's.  Workspace of esr_bisect_device_workspace_bytes(n, m,
+ * max_part) bytes (-1: sizes out of range).  Reads one 4-byte error count
+ * back (synchronises the stream once).  No reference counterpart. */
+int64_t esr_bisect_device_workspace_bytes(int64_t n, int64_t m,
+                                          int64_t max_part);
+int esr_bisect_partition_device(int64_t n, int64_t m, const int64_t *src,
+                                const int64_t *dst, int64_t max_part,
+                                int32_t *part, int64_t *nparts,
+                                void *workspace, int64_t workspace_bytes,
+                                void *stream);
 
 /* Host: the arrays of esr_swe_tiles from face slots nbr [3][nc] in a
  * tile-major numbering and the non-decreasing tile id of every cell.  Call

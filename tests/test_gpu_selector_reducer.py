@@ -159,3 +159,38 @@ def test_full_size_edge_exchange_properties():
     w = torch.rand(len(src), dtype=torch.float64, generator=torch.Generator().manual_seed(0))
     cell = mod.red(w.cuda())
     assert abs(float(cell.sum()) - float(w.sum())) <= 1e-9 * float(w.sum())
+
+
+def test_reducer_csr_built_on_the_device_equals_the_host_csr():
+    """compile for CUDA builds each Reducer's stable CSR with a device sort:
+    the same rowptr/perm as esr_csr_from_index on the host."""
+    from easier_gb300 import mesh
+
+    class M(esr.Module):
+        def __init__(self):
+            super().__init__()
+            g = torch.Generator().manual_seed(3)
+            self.idx = torch.randint(0, 5000, (200_003,), generator=g)
+            self.red = esr.Reducer(self.idx, 5000)
+            self.x = esr.Tensor(torch.randn(200_003, generator=g, dtype=torch.float64), mode="partition")
+
+        def forward(self):
+            return self.red(self.x)
+
+    m = M()
+    [m] = esr.compile([m], "cuda")
+    rowptr, perm = mesh.csr_from_index(m.idx.numpy(), 5000)
+    assert np.array_equal(m.red._rowptr32.cpu().numpy(), rowptr.astype(np.int32))
+    assert np.array_equal(m.red._perm32.cpu().numpy(), perm.astype(np.int32))
+
+
+def test_reducer_index_out_of_range_fails_at_compile():
+    from easier_gb300.utils import EasierJitException
+
+    class M(esr.Module):
+        def __init__(self):
+            super().__init__()
+            self.red = esr.Reducer(torch.tensor([0, 3, 9]), 4)
+
+    with pytest.raises(EasierJitException, match="out of range"):
+        esr.compile([M()], "cuda")

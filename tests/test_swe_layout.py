@@ -266,3 +266,77 @@ def test_fast_record_order_sorts_each_cells_slots():
         # same cell (column), ascending neighbours
         assert np.array_equal(np.sort(got, axis=0), np.sort(idx, axis=0))
         assert np.all(np.diff(lnbr[got], axis=0) >= 0)
+
+
+@pytest.mark.parametrize("n,tile", [(3, 8), (12, 100), (40, 700), (64, 1900)])
+def test_device_layout_functions_match_the_host_ones(n, tile):
+    """The torch layout path a CUDA engine runs on the GPU (cell slots, tile
+    rings, record order, slot_info), run here on CPU tensors with the host
+    partition: every array equals the host functions' (numpy / C++)."""
+    m = mesh.triangular_mesh(n)
+    src, dst, b = (np.asarray(a, np.int64) for a in (m.src, m.dst, m.bcells))
+    host = swe.cell_layout(m.nc, src, dst, b, reorder="tiles", tile_cells=tile)
+    dev = swe._cell_layout_device(m.nc, *(torch.from_numpy(a) for a in (src, dst, b)), "tiles", tile)
+    for k in ("order", "nbr", "pos", "part"):
+        assert np.array_equal(np.asarray(host[k]), dev[k].numpy()), k
+    assert host["width"] == dev["width"]
+    th = swe.tile_layout(host["nbr"], host["part"])
+    td = swe._tile_layout_device(dev["nbr"], dev["part"])
+    for k in ("meta", "off3", "offh", "halo", "lnbr", "slot_src", "area_src"):
+        assert np.array_equal(np.asarray(th[k]), td[k].numpy()), k
+    assert th["stats"] == td["stats"]
+    oh = swe._slots_by_neighbour(th["meta"], th["off3"], th["lnbr"])
+    od = swe._slots_by_neighbour(td["meta"], td["off3"], td["lnbr"])
+    assert np.array_equal(oh, od.numpy())
+
+
+def test_device_tile_layout_rejects_bad_input():
+    m = mesh.triangular_mesh(6)
+    lay = swe.cell_layout(m.nc, m.src, m.dst, m.bcells, reorder="tiles", tile_cells=20)
+    nbr, part = torch.from_numpy(lay["nbr"]), torch.from_numpy(lay["part"])
+    with pytest.raises(ValueError, match="non-decreasing"):
+        swe._tile_layout_device(nbr, part.flip(0))
+    bad = nbr.clone()
+    bad[0, 3] = m.nc
+    with pytest.raises(ValueError, match="out of range"):
+        swe._tile_layout_device(bad, part)
+    skip = part.clone()
+    skip[part >= 1] += 1
+    with pytest.raises(ValueError, match="skip"):
+        swe._tile_layout_device(nbr, skip)
+
+
+@pytest.mark.parametrize("as_torch", [False, True])
+def test_split_wide_tiles_cuts_the_tiles_over_the_limit(as_torch):
+    """Tiles whose local list exceeds the limit are each cut in two (new
+    tiles after the others); the rest keep their cells."""
+    m = mesh.triangular_mesh(40)
+    src, dst, b = (np.asarray(a, np.int64) for a in (m.src, m.dst, m.bcells))
+    conv = (lambda a: torch.from_numpy(a)) if as_torch else (lambda a: a)
+    lay = (swe._cell_layout_device(m.nc, conv(src), conv(dst), conv(b), "tiles", 600) if as_torch else
+           swe.cell_layout(m.nc, src, dst, b, reorder="tiles", tile_cells=600))
+    tiles = (swe._tile_layout_device if as_torch else swe.tile_layout)(lay["nbr"], lay["part"])
+    meta = np.asarray(tiles["meta"])
+    nl = meta[:, 5]
+    limit = int(np.sort(nl)[-3])  # the two widest tiles exceed it
+    wide = np.nonzero(nl > limit)[0]
+    assert wide.size == 2
+    assert swe.split_wide_tiles(lay, tiles, int(nl.max())) is None
+    part = swe.split_wide_tiles(lay, tiles, limit)
+    part = np.asarray(part)
+    order = np.asarray(lay["order"])
+    old = np.empty(m.nc, np.int64)
+    old[order] = np.asarray(lay["part"])
+    ntiles = meta.shape[0]
+    assert part.max() == ntiles + 1
+    for j, t in enumerate(wide):
+        cells = old == t
+        assert set(np.unique(part[cells])) == {t, ntiles + j}
+        sizes = np.bincount(part[cells] == t)
+        assert abs(int(sizes[0]) - int(sizes[1])) <= 1
+    keep = ~np.isin(old, wide)
+    assert np.array_equal(part[keep], old[keep])
+    lay2 = (swe._cell_layout_device(m.nc, conv(src), conv(dst), conv(b), "tiles", None, conv(part)) if as_torch else
+            swe.cell_layout(m.nc, src, dst, b, reorder="tiles", part=part))
+    st2 = (swe._tile_layout_device if as_torch else swe.tile_layout)(lay2["nbr"], lay2["part"])["stats"]
+    assert st2["ntiles"] == ntiles + 2 and st2["max_local"] < int(nl.max())
