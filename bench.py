@@ -320,29 +320,34 @@ def bench_swe(args, world, rank, local):
     achieved = bytes_step / (ms / args.steps / 1e3) / 1e9
     secondary = swe_secondary(args, eng, dev, stream) if args.dtype == "f32" else {}
 
-    # end to end through the C ABI with host buffers: every step uploads the
-    # state (h, uh, vh per cell: 12 bytes, the 4th lane of the device layout
-    # is padding) from pinned host memory, runs one step, reads it back
+    # end to end with the state in host memory: every step uploads the state
+    # (h, uh, vh per cell: 12 bytes, the 4th lane of the device layout is
+    # padding) from pinned host memory, runs one step and reads it back --
+    # through esr_swe_host_step (the tiled layout: chunked copies, the link
+    # used both ways), else the plain C-ABI step between two copies
     host = torch.empty((nc, 3), dtype=dtype, pin_memory=True)
     host.copy_(eng.state[:, :3])
-    stage = torch.empty((nc, 3), dtype=dtype, device=dev)
     ke = max(1, min(args.steps, args.e2e_steps))
-    a = eng.bufs[0]
-    b = eng.bufs[1] if eng.tiled else eng.bufs[0]
+    if eng.tiled:
+        eng.step_host(host, 1)  # plan set up outside the timed region
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     e0.record(stream)
-    for _ in range(ke):
-        stage.copy_(host, non_blocking=True)
-        a[:, :3].copy_(stage)
-        if eng.tiled:
-            _lib.call("esr_swe_tile_step", ctypes.byref(eng._tiles), float(args.dt), _lib.ptr(a), _lib.ptr(b), 1,
-                      stream.cuda_stream)
-        else:
+    if eng.tiled:
+        eng.step_host(host, ke)
+        path = ("SweEngine.step_host -> esr_swe_host_step (8 chunks a step; uploads, downloads and the step's "
+                "tile groups overlapped)")
+    else:
+        stage = torch.empty((nc, 3), dtype=dtype, device=dev)
+        a = eng.bufs[0]
+        for _ in range(ke):
+            stage.copy_(host, non_blocking=True)
+            a[:, :3].copy_(stage)
             _lib.call("esr_swe_step", ctypes.byref(eng._mesh), float(args.dt), _lib.ptr(a), 1,
                       _lib.ptr(eng.ws), stream.cuda_stream)
-        stage.copy_(b[:, :3])
-        host.copy_(stage, non_blocking=True)
+            stage.copy_(a[:, :3])
+            host.copy_(stage, non_blocking=True)
+        path = "esr_swe_step via ctypes between copies of the state from/to pinned host memory"
     e1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1)
@@ -350,9 +355,7 @@ def bench_swe(args, world, rank, local):
     e2e_ms = _max_over_ranks(world, max(e2e_ms, e2e_wall * 1e3))
     e2e = {"value": world * nc * ke / (e2e_ms / 1e3), "unit": "cell-steps/s",
            "h2d_bytes_per_step": host.numel() * host.element_size(),
-           "d2h_bytes_per_step": host.numel() * host.element_size(), "steps": ke,
-           "path": ("esr_swe_tile_step" if eng.tiled else "esr_swe_step") +
-                   " via ctypes, state (h, uh, vh) [nc,3] from/to pinned host memory each step"}
+           "d2h_bytes_per_step": host.numel() * host.element_size(), "steps": ke, "path": path}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -117,6 +117,9 @@ _SIGS = {
     "esr_swe_tile_kernel": (c_int, [POINTER(SweTiles)]),
     "esr_swe_tile_step_with": (c_int, [POINTER(SweTiles), c_int, c_double, _P, _P, c_int64, _P]),
     "esr_bisect_partition": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P]),
+    "esr_swe_host_plan_create": (c_int, [POINTER(SweTiles), _P, _P, _P, _P, c_int32, POINTER(c_void_p)]),
+    "esr_swe_host_step": (c_int, [_P, c_double, _P, c_int64, _P]),
+    "esr_swe_host_plan_destroy": (c_int, [_P]),
     "esr_bisect_device_workspace_bytes": (c_int64, [c_int64, c_int64, c_int64]),
     "esr_bisect_partition_device": (c_int, [c_int64, c_int64, _P, _P, c_int64, _P, _P, _P, c_int64, _P]),
     "esr_swe_tile_layout": (c_int, [c_int64, _P, _P, c_int64, _P, POINTER(c_int64), POINTER(c_int64), _P, _P, _P,

@@ -33,7 +33,9 @@
 //   2: D2 = delta(S1);           S2 = s0 + c1*D2;  A = A + D2
 //   3: D3 = delta(S2);           S1 = s0 + c3*D3;  A = A + D3
 //   4: D4 = delta(S1);           s0 = s0 + c4*(A + D4)
+#include <algorithm>
 #include <cstdint>
+#include <vector>
 
 #include "esr_internal.h"
 #include "reduce_util.cuh"
@@ -935,13 +937,14 @@ __global__ void __launch_bounds__(TT, 1)
 swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict__ off3,
                      const int64_t *__restrict__ offh, const int32_t *__restrict__ halo,
                      const float4 *__restrict__ gslot, const float4 *__restrict__ sin, float4 *__restrict__ sout,
-                     int64_t nc, int ntiles, float c1, float c3, float c4) {
+                     int64_t nc, int ntiles, float c1, float c3, float c4, const int32_t *__restrict__ tile_ids) {
+  // tile_ids (optional): the tiles this launch walks, ntiles of them
   using namespace pipe;
   extern __shared__ float smem[];
   const Buf SA{smem + 2 * kBuf}, SB{smem + 3 * kBuf};
   int t = blockIdx.x;
   if (t >= ntiles) return;
-  TileMeta m = tile_meta(meta, off3, offh, t);
+  TileMeta m = tile_meta(meta, off3, offh, tile_ids ? __ldg(tile_ids + t) : t);
   constexpr int kMaxOwnT = TT * CELLS;  // the tile's cells are among the register-held ones
   bool fits = tile_fits(m, nc, kMaxOwnT);
   int cur = 0;
@@ -961,7 +964,7 @@ swe_tile_pipe_kernel(const int32_t *__restrict__ meta, const int64_t *__restrict
     TileMeta mn{};
     bool next = tn < ntiles;
     if (next) {
-      mn = tile_meta(meta, off3, offh, tn);
+      mn = tile_meta(meta, off3, offh, tile_ids ? __ldg(tile_ids + tn) : tn);
       if (!tile_fits(mn, nc, kMaxOwnT)) {  // outside the kernel's limits: flag it, leave its cells unwritten
         esr::raise_status(ESR_DEV_IDX_RANGE);
       }
@@ -1017,9 +1020,10 @@ bool pipe_fits(const esr_swe_tiles *T, int shape) {
 
 int pipe_shape(const esr_swe_tiles *) { return ESR_SWE_TILE_PIPELINED_512; }
 
+// (tile_ids: the launch walks those `count` tiles only)
 template <int TT, int CELLS>
 int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
-                   cudaStream_t s) {
+                   cudaStream_t s, const int32_t *tile_ids = nullptr, int count = 0) {
   cudaError_t e = cudaFuncSetAttribute(swe_tile_pipe_kernel<TT, CELLS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, pipe::kSmemBytes);
   if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/pipelined smem attribute");
@@ -1027,13 +1031,15 @@ int run_pipe_shape(const esr_swe_tiles *tiles, double dt, void *state_a, void *s
   e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_tile_step/SM count");
-  const int grid = tiles->ntiles < sms ? tiles->ntiles : sms;
+  const int nt = tile_ids ? count : tiles->ntiles;
+  if (nt <= 0) return ESR_OK;
+  const int grid = nt < sms ? nt : sms;
   const float c1 = (float)(0.5 * dt), c3 = (float)dt, c4 = (float)(dt / 6);
   float4 *buf[2] = {(float4 *)state_a, (float4 *)state_b};
   for (int64_t k = 0; k < steps; ++k) {
     swe_tile_pipe_kernel<TT, CELLS><<<grid, TT, pipe::kSmemBytes, s>>>(
         tiles->meta, tiles->off3, tiles->offh, tiles->halo, (const float4 *)tiles->slots, buf[k & 1],
-        buf[(k + 1) & 1], tiles->nc, tiles->ntiles, c1, c3, c4);
+        buf[(k + 1) & 1], tiles->nc, nt, c1, c3, c4, tile_ids);
   }
   ESR_LAUNCH_CHECK("esr_swe_tile_step/pipelined");
   return ESR_OK;
@@ -1127,4 +1133,235 @@ extern "C" int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, do
 extern "C" int esr_swe_tile_step(const esr_swe_tiles *tiles, double dt, void *state_a, void *state_b, int64_t steps,
                                  void *stream) {
   return esr_swe_tile_step_with(tiles, ESR_SWE_TILE_AUTO, dt, state_a, state_b, steps, stream);
+}
+
+// ------------------------------------------------------------------------
+// A state held in host memory, stepped on the GPU.  Per step the FP32
+// (h, uh, vh) [nc][3] state goes up in chunks (copy stream `up`), each chunk
+// is unpacked into the [nc] float4 engine layout as it lands, the step runs
+// on the caller's stream, and each chunk is packed and brought back (copy
+// stream `down`) as soon as it is packed.  The next step's upload of a
+// chunk waits only for that chunk's download, so while chunk c of a result
+// comes home chunk c - 1 of the next step's input goes up: the link carries
+// both directions at once.
+namespace {
+
+__global__ void unpack3_kernel(const float *__restrict__ stage, float4 *__restrict__ a, int64_t off, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float *q = stage + 3 * (off + i);
+    a[off + i] = make_float4(q[0], q[1], q[2], 0.f);
+  }
+}
+
+__global__ void pack3_kernel(const float4 *__restrict__ b, float *__restrict__ stage, int64_t off, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4 v = b[off + i];
+    float *q = stage + 3 * (off + i);
+    q[0] = v.x;
+    q[1] = v.y;
+    q[2] = v.z;
+  }
+}
+
+struct SweHostPlan {
+  esr_swe_tiles tiles{};
+  float4 *a = nullptr, *b = nullptr;
+  float *stage = nullptr;
+  int chunks = 0;
+  int grid = 0;
+  std::vector<int64_t> off;  // [chunks + 1] cell offsets, multiples of 4
+  cudaStream_t up = nullptr, down = nullptr;
+  cudaEvent_t entry = nullptr;
+  std::vector<cudaEvent_t> ev_up, ev_pack, ev_down;
+  // grouped schedule (pipelined kernel): the tiles whose local cells all lie
+  // in chunks <= g form group g (tile_list[group_off[g] .. group_off[g+1]])
+  // and run as soon as chunk g has landed; chunk c goes home after group
+  // ready[c], the last one holding tiles that own cells of chunk c
+  const int32_t *tile_list = nullptr;
+  std::vector<int32_t> group_off, ready;
+};
+
+// the grouped schedule of a plan from the layout (read back once)
+int plan_groups(SweHostPlan *P, int32_t *tile_list) {
+  const esr_swe_tiles &T = P->tiles;
+  const int C = P->chunks;
+  const int nt = T.ntiles;
+  std::vector<int32_t> meta(8 * (size_t)nt);
+  std::vector<int64_t> offh(nt);
+  cudaError_t e = cudaMemcpy(meta.data(), T.meta, meta.size() * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(offh.data(), T.offh, offh.size() * 8, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_host_plan_create/layout");
+  int64_t th = 0;
+  for (int t = 0; t < nt; ++t) th = std::max(th, offh[t] + (int64_t)(meta[8 * t + 5] - meta[8 * t + 1]));
+  std::vector<int32_t> halo(th > 0 ? th : 1);
+  if (th > 0) e = cudaMemcpy(halo.data(), T.halo, th * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_host_plan_create/halo");
+  const int64_t per = P->off[1];  // every chunk but the last has `per` cells
+  auto chunk = [&](int64_t cell) { return (int)std::min<int64_t>(cell / per, C - 1); };
+  std::vector<int32_t> group(nt);
+  P->ready.assign(C, 0);
+  for (int t = 0; t < nt; ++t) {
+    const int64_t c0 = meta[8 * t], n0 = meta[8 * t + 1], nl = meta[8 * t + 5];
+    if (n0 <= 0) {
+      group[t] = 0;
+      continue;
+    }
+    int g = chunk(c0 + n0 - 1);
+    for (int64_t j = 0; j < nl - n0; ++j) {
+      const int64_t cell = halo[offh[t] + j];
+      if (cell >= 0 && cell < T.nc) g = std::max(g, chunk(cell));
+    }
+    group[t] = g;
+    for (int c = chunk(c0); c <= chunk(c0 + n0 - 1); ++c) P->ready[c] = std::max(P->ready[c], g);
+  }
+  P->group_off.assign(C + 1, 0);
+  for (int t = 0; t < nt; ++t) P->group_off[group[t] + 1]++;
+  for (int g = 0; g < C; ++g) P->group_off[g + 1] += P->group_off[g];
+  std::vector<int32_t> list(nt), fill(P->group_off.begin(), P->group_off.end() - 1);
+  for (int t = 0; t < nt; ++t) list[fill[group[t]]++] = t;
+  e = cudaMemcpy(tile_list, list.data(), (size_t)nt * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_host_plan_create/tile list");
+  P->tile_list = tile_list;
+  return ESR_OK;
+}
+
+void destroy_host_plan(SweHostPlan *P) {
+  if (!P) return;
+  for (auto *v : {&P->ev_up, &P->ev_pack, &P->ev_down})
+    for (cudaEvent_t e : *v)
+      if (e) cudaEventDestroy(e);
+  if (P->entry) cudaEventDestroy(P->entry);
+  if (P->up) cudaStreamDestroy(P->up);
+  if (P->down) cudaStreamDestroy(P->down);
+  delete P;
+}
+
+}  // namespace
+
+extern "C" int esr_swe_host_plan_create(const esr_swe_tiles *tiles, void *state_a, void *state_b, void *staging,
+                                        int32_t *tile_list, int32_t chunks, void **plan_out) {
+  int st = check_tiles(tiles);
+  if (st) return st;
+  if (!state_a || !state_b || !staging || !plan_out || state_a == state_b)
+    return esr::fail(ESR_ERR_ARG, "need two distinct state buffers, a staging buffer and an output pointer");
+  if (((uintptr_t)state_a | (uintptr_t)state_b) % 16 || (uintptr_t)staging % 16)
+    return esr::fail(ESR_ERR_ARG, "state and staging buffers must be 16-byte aligned");
+  if (chunks < 1 || chunks > 64) return esr::fail(ESR_ERR_ARG, "chunks must be in [1, 64]");
+  SweHostPlan *P = new (std::nothrow) SweHostPlan();
+  if (!P) return esr::fail(ESR_ERR_ARG, "out of host memory");
+  try {
+    P->tiles = *tiles;
+    P->a = (float4 *)state_a;
+    P->b = (float4 *)state_b;
+    P->stage = (float *)staging;
+    const int64_t nc = tiles->nc;
+    const int64_t per = ((nc + chunks - 1) / chunks + 3) / 4 * 4;
+    P->off.push_back(0);
+    while (P->off.back() < nc) P->off.push_back(std::min(nc, P->off.back() + per));
+    P->chunks = (int)P->off.size() - 1;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->down, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->entry, cudaEventDisableTiming);
+    P->grid = 4 * (sms > 0 ? sms : 1);
+    for (auto *v : {&P->ev_up, &P->ev_pack, &P->ev_down}) {
+      v->assign(P->chunks, nullptr);
+      for (int c = 0; c < P->chunks && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&(*v)[c], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+      destroy_host_plan(P);
+      return esr::cuda_check(e, "esr_swe_host_plan_create");
+    }
+    if (tile_list && P->chunks > 1 && pipe_fits(tiles, ESR_SWE_TILE_PIPELINED_512)) {
+      const int gst = plan_groups(P, tile_list);
+      if (gst) {
+        destroy_host_plan(P);
+        return gst;
+      }
+    }
+  } catch (const std::bad_alloc &) {
+    destroy_host_plan(P);
+    return esr::fail(ESR_ERR_ARG, "out of host memory");
+  }
+  *plan_out = P;
+  return ESR_OK;
+}
+
+extern "C" int esr_swe_host_step(void *plan, double dt, float *host_state, int64_t steps, void *stream) {
+  if (!plan || !host_state) return esr::fail(ESR_ERR_ARG, "null plan or host state");
+  if (steps < 0) return esr::fail(ESR_ERR_ARG, "negative step count");
+  if (steps == 0) return ESR_OK;
+  SweHostPlan *P = (SweHostPlan *)plan;
+  cudaStream_t s = esr::as_stream(stream);
+  const int C = P->chunks;
+  // the uploads overwrite the staging buffer: after the caller's earlier work
+  cudaError_t e = cudaEventRecord(P->entry, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(P->up, P->entry, 0);
+  for (int64_t k = 0; k < steps && e == cudaSuccess; ++k) {
+    for (int c = 0; c < C && e == cudaSuccess; ++c) {
+      const int64_t o = P->off[c], n = P->off[c + 1] - o;
+      if (k > 0) e = cudaStreamWaitEvent(P->up, P->ev_down[c], 0);  // chunk c of the last result is home
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(P->stage + 3 * o, host_state + 3 * o, 12 * n, cudaMemcpyHostToDevice, P->up);
+      if (e == cudaSuccess) e = cudaEventRecord(P->ev_up[c], P->up);
+    }
+    auto unpack = [&](int c) {
+      const int64_t o = P->off[c], n = P->off[c + 1] - o;
+      cudaError_t r = cudaStreamWaitEvent(s, P->ev_up[c], 0);
+      if (r == cudaSuccess) {
+        unpack3_kernel<<<P->grid, 256, 0, s>>>(P->stage, P->a, o, n);
+        r = cudaGetLastError();
+      }
+      return r;
+    };
+    auto pack = [&](int c) {
+      const int64_t o = P->off[c], n = P->off[c + 1] - o;
+      pack3_kernel<<<P->grid, 256, 0, s>>>(P->b, P->stage, o, n);
+      cudaError_t r = cudaGetLastError();
+      if (r == cudaSuccess) r = cudaEventRecord(P->ev_pack[c], s);
+      return r;
+    };
+    if (P->tile_list) {  // each group of tiles as soon as its chunks have landed
+      for (int g = 0; g < C && e == cudaSuccess; ++g) {
+        e = unpack(g);
+        if (e != cudaSuccess) break;
+        const int st = run_pipe_shape<512, 4>(&P->tiles, dt, P->a, P->b, 1, s, P->tile_list + P->group_off[g],
+                                              P->group_off[g + 1] - P->group_off[g]);
+        if (st) return st;
+        for (int c = 0; c < C && e == cudaSuccess; ++c)
+          if (P->ready[c] == g) e = pack(c);
+      }
+    } else {
+      for (int c = 0; c < C && e == cudaSuccess; ++c) e = unpack(c);
+      if (e != cudaSuccess) break;
+      const int st = esr_swe_tile_step_with(&P->tiles, ESR_SWE_TILE_AUTO, dt, P->a, P->b, 1, s);
+      if (st) return st;
+      for (int c = 0; c < C && e == cudaSuccess; ++c) e = pack(c);
+    }
+    for (int c = 0; c < C && e == cudaSuccess; ++c) {
+      const int64_t o = P->off[c], n = P->off[c + 1] - o;
+      e = cudaStreamWaitEvent(P->down, P->ev_pack[c], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_state + 3 * o, P->stage + 3 * o, 12 * n, cudaMemcpyDeviceToHost, P->down);
+      if (e == cudaSuccess) e = cudaEventRecord(P->ev_down[c], P->down);
+    }
+  }
+  // the caller's stream sees the last result home
+  for (int c = 0; c < C && e == cudaSuccess; ++c) e = cudaStreamWaitEvent(s, P->ev_down[c], 0);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_host_step");
+  return ESR_OK;
+}
+
+extern "C" int esr_swe_host_plan_destroy(void *plan) {
+  if (!plan) return ESR_OK;
+  SweHostPlan *P = (SweHostPlan *)plan;
+  cudaError_t e = cudaStreamSynchronize(P->up);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->down);
+  destroy_host_plan(P);
+  if (e != cudaSuccess) return esr::cuda_check(e, "esr_swe_host_plan_destroy");
+  return ESR_OK;
 }

@@ -73,6 +73,8 @@ LAYOUT_ON_DEVICE = True
 # (<= 2048 own cells, <= 4096 local cells)
 PIPE_TILE_TARGET = 1900
 PIPE_LIMITS = dict(max_own=2048, max_local=4096)
+# pieces a host-resident state moves in per step (step_host)
+HOST_CHUNKS = 8
 # tile kernel: "auto" (pipelined where the layout allows), "blocked",
 # "pipelined" (its shape from the tile size), "pipelined_512", "pipelined_768"
 DEFAULT_TILE_KERNEL = "auto"
@@ -245,6 +247,8 @@ class SweEngine:
         self.tile_cells = min(tile_cells or DEFAULT_TILE_CELLS or self._auto_tile_cells(), TILE_CELLS)
         self.mode = mode
         self.tile_kernel = DEFAULT_TILE_KERNEL
+        self._host_plan = None
+        self._host_stage = None
         self._dt_attr = binding.get("dt_attr", "dt")
         self._build_layout()
 
@@ -454,6 +458,47 @@ class SweEngine:
         _lib.call("esr_swe_delta", ctypes.byref(self._mesh), _lib.ptr(state), _lib.ptr(out),
                   _lib.stream_handle(self.device))
         return out
+
+    def step_host(self, host: torch.Tensor, steps: int = 1, chunks: int = HOST_CHUNKS) -> None:
+        """Advance a state kept in host memory: ``host`` is FP32 (h, uh, vh)
+        [nc, 3] in the engine's cell numbering (``self.order``), updated in
+        place (pinned memory lets the copies overlap).  Every step uploads
+        it, runs one fused step and brings the result back, in ``chunks``
+        pieces so that uploads and downloads share the host link both ways
+        (esr_swe_host_step); with the pipelined kernel the step's tiles also
+        run in groups as their chunks land.  Returns once ``host`` holds the
+        result; the engine's device state then holds it too."""
+        if not self.tiled:
+            raise NotImplementedError("host-resident stepping needs the tiled FP32 layout")
+        if (host.dtype != torch.float32 or tuple(host.shape) != (self.nc, 3) or host.is_cuda
+                or not host.is_contiguous()):
+            raise ValueError(f"host state must be a contiguous CPU float32 tensor of shape ({self.nc}, 3)")
+        self._sync_inputs()  # (may rebuild the geometry records the plan points to)
+        key = (self.t_slots.data_ptr(), self.bufs[0].data_ptr(), self.bufs[1].data_ptr(), int(chunks))
+        if self._host_plan is None or self._host_plan[0] != key:
+            self._free_host_plan()
+            if self._host_stage is None:
+                self._host_stage = torch.empty((self.nc, 3), dtype=torch.float32, device=self.device)
+                self._host_tiles = torch.empty(self.ntiles, dtype=torch.int32, device=self.device)
+            h = ctypes.c_void_p()
+            _lib.call("esr_swe_host_plan_create", ctypes.byref(self._tiles), _lib.ptr(self.bufs[0]),
+                      _lib.ptr(self.bufs[1]), _lib.ptr(self._host_stage), _lib.ptr(self._host_tiles), int(chunks),
+                      ctypes.byref(h))
+            self._host_plan = (key, h)
+        stream = torch.cuda.current_stream(self.device)
+        _lib.call("esr_swe_host_step", self._host_plan[1], self.dt, _lib.ptr(host), int(steps),
+                  _lib.stream_handle(self.device))
+        stream.synchronize()
+        self.cur = 1
+        self._bind_views()
+
+    def _free_host_plan(self) -> None:
+        if getattr(self, "_host_plan", None) is not None:
+            try:
+                _lib.call("esr_swe_host_plan_destroy", self._host_plan[1])
+            except Exception:  # interpreter shutdown
+                pass
+        self._host_plan = None
 
     def launches_per_step(self) -> int:
         return 1 if self.tiled else 4

@@ -381,6 +381,32 @@ int esr_swe_tile_step_with(const esr_swe_tiles *tiles, int kernel, double dt,
                            void *state_a, void *state_b, int64_t steps,
                            void *stream);
 
+/* A shallow-water state held in host memory, stepped on the GPU (no
+ * reference counterpart; the round trip of a user who keeps the state on
+ * the host).  host_state is FP32 (h, uh, vh) [nc][3] in the tiled layout's
+ * cell numbering (pinned memory for overlap).  Per step the state goes up
+ * in `chunks` pieces (each unpacked into state_a, [nc] x 16 bytes, as it
+ * lands), esr_swe_tile_step advances state_a into state_b, and each piece
+ * is packed and brought back as soon as it is ready; a piece's upload for
+ * the next step waits only for its own download, so uploads and downloads
+ * share the host link in both directions.  staging: [nc][3] FP32 device
+ * scratch.  tile_list (optional, [ntiles] int32 device scratch): when the
+ * pipelined kernel takes the layout, the step itself overlaps the copies --
+ * the tiles whose local cells all lie in the first g+1 chunks run as soon as
+ * chunk g has landed, and a chunk goes home as soon as the tiles owning its
+ * cells have run (results bitwise those of esr_swe_tile_step); the plan
+ * reads the layout's meta, offh and halo back once to group the tiles.
+ * The plan keeps a copy of *tiles (its arrays must outlive it) and owns two
+ * copy streams and per-chunk events.  esr_swe_host_step returns with the
+ * work enqueued: host_state holds the result once `stream` is
+ * synchronised. */
+int esr_swe_host_plan_create(const esr_swe_tiles *tiles, void *state_a,
+                             void *state_b, void *staging, int32_t *tile_list,
+                             int32_t chunks, void **plan_out);
+int esr_swe_host_step(void *plan, double dt, float *host_state, int64_t steps,
+                      void *stream);
+int esr_swe_host_plan_destroy(void *plan);
+
 /* Host: partition an undirected graph (directed edge lists) into parts of at
  * most max_part vertices by recursive BFS bisection (compact parts; a set
  * due to end as k = ceil(size / max_part) parts is split floor(k/2) : ceil(k/2),

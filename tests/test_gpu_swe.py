@@ -318,3 +318,31 @@ def test_engine_finds_roles_of_a_renamed_module(dtype):
         tut()
     for a, b in (("depth", "h"), ("p", "uh"), ("q", "vh")):
         assert torch.equal(getattr(ren, a).collect().cpu(), getattr(tut, b).collect().cpu()), a
+
+
+@pytest.mark.parametrize("precision", ["fast", "exact"])
+def test_host_resident_stepping_equals_device_stepping(precision):
+    """SweEngine.step_host (esr_swe_host_step: chunked uploads and downloads
+    of a state in pinned host memory, overlapped both ways) gives bitwise
+    the device-resident steps, for any chunk count, and leaves the module's
+    views on the result."""
+    eqn = workloads.make_swe(150, dt=5e-4, dtype=torch.float32)
+    [eqn] = esr.compile([eqn], "cuda", precision=precision)
+    eng = eqn.easier_fused_engine
+    assert eng.tiled
+    s0 = eng.state.clone()
+    eng.step(5)
+    torch.cuda.synchronize()
+    want = eng.state[:, :3].cpu()
+    for chunks in (1, 3, 8):
+        eng.state.copy_(s0)
+        host = torch.empty((eng.nc, 3), dtype=torch.float32, pin_memory=True)
+        host.copy_(s0[:, :3].cpu())
+        eng.step_host(host, 5, chunks=chunks)
+        assert torch.equal(host, want), chunks
+        assert torch.equal(eng.state[:, :3].cpu(), want)
+        h = torch.empty_like(want[:, 0])
+        h[eng.order.cpu()] = want[:, 0]
+        assert torch.equal(eqn.h.collect().cpu(), h)
+    with pytest.raises(ValueError):
+        eng.step_host(torch.zeros((eng.nc, 4)), 1)
