@@ -329,14 +329,14 @@ def bench_swe(args, world, rank, local):
     host.copy_(eng.state[:, :3])
     ke = max(1, min(args.steps, args.e2e_steps))
     if eng.tiled:
-        eng.step_host(host, 1)  # plan set up outside the timed region
+        eng.step_host(host, 1, chunks=args.host_chunks)  # plan set up outside the timed region
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     e0.record(stream)
     if eng.tiled:
-        eng.step_host(host, ke)
-        path = ("SweEngine.step_host -> esr_swe_host_step (8 chunks a step; uploads, downloads and the step's "
-                "tile groups overlapped)")
+        eng.step_host(host, ke, chunks=args.host_chunks)
+        path = (f"SweEngine.step_host -> esr_swe_host_step ({args.host_chunks} chunks a step; uploads, downloads "
+                "and the step's tile groups overlapped)")
     else:
         stage = torch.empty((nc, 3), dtype=dtype, device=dev)
         a = eng.bufs[0]
@@ -977,12 +977,16 @@ def main():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-solvers", action="store_true", help="swe: leave out the solver figures")
     ap.add_argument("--tile-cells", type=int, default=None, help="swe: target cells per tile (FP32 tiled step)")
+    ap.add_argument("--host-chunks", type=int, default=None, help="swe: pieces of the end-to-end state copies")
     ap.add_argument("--tile-kernel", default=None,
                     choices=["auto", "blocked", "pipelined", "pipelined_512", "pipelined_768"],
                     help="swe: tile kernel of the FP32 tiled step")
     args = ap.parse_args()
     if args.n is None:
         args.n = {"swe": 2000, "poisson-fv": 500}.get(args.workload, 1000)
+    if args.host_chunks is None:
+        from easier_gb300 import swe as _swe
+        args.host_chunks = _swe.HOST_CHUNKS
     if args.dt is None:
         # dt = 5e-4 at N=2000 exceeds the scheme's stability limit (the state
         # turns non-finite within ~200 steps); 2.5e-4 is stable for 1000+
