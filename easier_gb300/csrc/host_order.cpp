@@ -235,25 +235,32 @@ extern "C" int esr_sell_build(int64_t n, const int64_t *rowptr, const int64_t *p
   ESR_HOST_CATCH
 }
 
-// Recursive BFS bisection: split a vertex set in two by the first half of a
-// BFS order started from a pseudo-peripheral vertex of the set (two sweeps),
-// recurse until every part has at most max_part vertices.  Parts are
-// compact (BFS slabs alternate direction as they shrink) and equal-sized
-// within one vertex.  Deterministic.  part[v] = part number; parts are
-// numbered in depth-first order of the recursion.
+// Recursive BFS bisection: split a vertex set in two along the BFS
+// distances from a pseudo-peripheral vertex of the set, recurse until every
+// part has at most max_part vertices.  The pseudo-peripheral vertex is the
+// one farthest (largest distance, then smallest id) from the set's first
+// vertex; the set is then ordered by (distance from it, id), unreached
+// vertices (another component) last by id, and a set due to end as
+// k = ceil(size / max_part) parts keeps its first size * floor(k/2) / k
+// vertices on the left.  Parts are compact and equal-sized within one
+// vertex; part ids are numbered in depth-first order.  Deterministic, and
+// the same partition as esr_bisect_partition_device (partition_gpu.cu),
+// which computes the same distances and order on the GPU.
 namespace {
+
+constexpr int64_t kUnreached = INT64_MAX;
 
 // Recursive BFS bisection over disjoint ranges of `verts`.  A range's
 // vertices carry its label; ranges of one level touch disjoint vertices, so
 // subtrees run on separate threads: label is read across ranges (a
 // neighbour's) while its owner relabels it, hence relaxed atomic accesses
 // (the value read is never the reader's own id either way).  Labels are
-// heap-numbered (children of id: 2 id + 1, 2 id + 2) and BFS stamps are
-// 3 id + sweep, so no counter is shared; part ids come from each range's
-// first part and part count, in left-to-right order.
+// heap-numbered (children of id: 2 id + 1, 2 id + 2), so no counter is
+// shared; part ids come from each range's first part and part count, in
+// left-to-right order.
 struct Bisector {
   const std::vector<int64_t> &ptr, &adj;
-  std::vector<int64_t> &label, &mark, &verts;
+  std::vector<int64_t> &label, &dist, &verts;
   int64_t *part;
   int64_t max_part;
   int par_depth;
@@ -261,31 +268,22 @@ struct Bisector {
   static int64_t ld(const int64_t *p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
   static void st(int64_t *p, int64_t v) { __atomic_store_n(p, v, __ATOMIC_RELAXED); }
 
-  // BFS order of verts[b:e] (all labelled id) from start; unreached
-  // vertices (other components) are appended in their current order
-  void bfs(int64_t b, int64_t e, int64_t id, int64_t start, int64_t stamp, std::vector<int64_t> &order) const {
-    order.clear();
-    order.push_back(start);
-    mark[start] = stamp;
-    size_t h = 0;
-    while (true) {
-      while (h < order.size()) {
-        const int64_t v = order[h++];
-        for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
-          const int64_t w = adj[k];
-          if (ld(&label[w]) == id && mark[w] != stamp) {
-            mark[w] = stamp;
-            order.push_back(w);
-          }
+  // BFS distances from start over the vertices labelled id (verts[b:e]);
+  // the others of the range stay kUnreached.  `queue` is scratch.
+  void distances(int64_t b, int64_t e, int64_t id, int64_t start, std::vector<int64_t> &queue) const {
+    for (int64_t i = b; i < e; ++i) dist[verts[i]] = kUnreached;
+    queue.clear();
+    queue.push_back(start);
+    dist[start] = 0;
+    for (size_t h = 0; h < queue.size(); ++h) {
+      const int64_t v = queue[h];
+      for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+        const int64_t w = adj[k];
+        if (ld(&label[w]) == id && dist[w] == kUnreached) {
+          dist[w] = dist[v] + 1;
+          queue.push_back(w);
         }
       }
-      if ((int64_t)order.size() == e - b) break;
-      for (int64_t i = b; i < e; ++i)
-        if (mark[verts[i]] != stamp) {
-          mark[verts[i]] = stamp;
-          order.push_back(verts[i]);
-          break;
-        }
     }
   }
 
@@ -295,18 +293,24 @@ struct Bisector {
       for (int64_t i = b; i < e; ++i) part[verts[i]] = first_part;
       return;
     }
-    // two sweeps find a vertex at a far end of the set (a pseudo-peripheral
-    // vertex); the BFS from there orders the set along its long axis, so the
-    // halves stay compact (one sweep leaves some long, thin parts)
-    std::vector<int64_t> order;
-    order.reserve(sz);
-    int64_t s = verts[b];
-    for (int sweep = 0; sweep < 2; ++sweep) {
-      bfs(b, e, id, s, 3 * id + sweep, order);
-      s = order.back();
+    // one sweep: the reached vertex farthest from the first one (largest
+    // distance, then smallest id); the distances from there order the set
+    std::vector<int64_t> queue;
+    queue.reserve(sz);
+    distances(b, e, id, verts[b], queue);
+    int64_t far = verts[b], fd = 0;
+    for (int64_t i = b; i < e; ++i) {
+      const int64_t v = verts[i], d = dist[v];
+      if (d != kUnreached && (d > fd || (d == fd && v < far))) {
+        far = v;
+        fd = d;
+      }
     }
-    bfs(b, e, id, s, 3 * id + 2, order);
-    std::copy(order.begin(), order.end(), verts.begin() + b);
+    distances(b, e, id, far, queue);
+    std::sort(verts.begin() + b, verts.begin() + e, [this](int64_t x, int64_t y) {
+      const int64_t dx = dist[x], dy = dist[y];
+      return dx != dy ? dx < dy : x < y;
+    });
     // the set ends as k = ceil(sz / max_part) parts: the first floor(k/2)
     // parts' share of it goes left, so every final part has about sz / k
     // vertices (not sz / 2^j: tiles come out close to max_part)
@@ -372,13 +376,13 @@ extern "C" int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src, co
       adj[pos[dst[e]]++] = src[e];
     }
   }
-  std::vector<int64_t> label(n, 0), mark(n, -1), verts(n);
+  std::vector<int64_t> label(n, 0), dist(n, kUnreached), verts(n);
   for (int64_t i = 0; i < n; ++i) verts[i] = i;
   // subtrees in parallel down to ~2 per hardware thread
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   int par_depth = 0;
   while ((1u << par_depth) < 2 * hw && par_depth < 8) ++par_depth;
-  Bisector bs{ptr, adj, label, mark, verts, part, max_part, par_depth};
+  Bisector bs{ptr, adj, label, dist, verts, part, max_part, par_depth};
   if (n > 0) bs.run(0, n, 0, 0, 0);
   *nparts = n > 0 ? (n + max_part - 1) / max_part : 0;
   return ESR_OK;

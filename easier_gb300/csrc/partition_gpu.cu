@@ -3,10 +3,10 @@
 // k = ceil(size / max_part) parts splits floor(k/2) : ceil(k/2) by size
 // along the BFS order from a pseudo-peripheral vertex, and the parts are
 // numbered left to right, i.e. in depth-first order.  The pseudo-peripheral
-// vertex comes from one sweep here (the vertex farthest from the set's
-// first one), not the host's two: as compact on the tutorial meshes
-// (level-<=3 cells per tile cell 1.208 vs 1.205 at N=1000, 1.211 vs 1.207 at
-// N=2000), a third fewer BFS levels.
+// vertex comes from one sweep (the vertex farthest from the set's first
+// one; two sweeps gave no more compact tiles on the tutorial meshes --
+// level-<=3 cells per tile cell 1.205 vs 1.208 at N=1000 -- for 50% more
+// BFS levels).
 //
 // GPU shape.  All sets ("segments") of one recursion depth are processed by
 // one launch, one thread-block cluster per segment (clusters of up to 8 CTAs
@@ -24,9 +24,8 @@
 // each depth orders every segment's vertices by (segment, distance) with one
 // radix sort, stable over vertex ids, and cuts the segments.  The result
 // depends only on BFS distances and ids, never on the order in which
-// threads discover vertices, so it is deterministic; it is not the host
-// partition (whose BFS orders a level by discovery), and it does not need
-// to be: any deterministic compact split serves the tile layout.
+// threads discover vertices: it is deterministic and vertex for vertex the
+// host function's, which takes the same steps serially.
 #include <cooperative_groups.h>
 
 #include <cstdint>

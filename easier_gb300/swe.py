@@ -65,6 +65,11 @@ DEFAULT_MODE = "auto"   # "auto" (tiled for FP32), "tiled" or "staged"
 # tile-major: the partition alone, without the RCM pass).  Measured at
 # N=2000: the same kernel time (0.454 vs 0.457 ms), 2 s less compile.
 TILED_REORDER = "tiles"
+# numbering of a staged (FP64) layout: "none" (the module's own order; built
+# on the device) or "rcm" (reverse Cuthill-McKee, a host pass).  Measured at
+# N=2000 on the tutorial mesh: the same step time (21.3 / 8.29 ms exact /
+# fast), 0.37 instead of 5.7 s of setup.
+STAGED_REORDER = "none"
 # build the tiled layout of a CUDA engine on the GPU (esr_bisect_partition_device
 # and torch sorts); False: the host functions (same arrays for the same
 # partition; the host partition itself differs, see esr_bisect_partition_device)
@@ -274,8 +279,9 @@ class SweEngine:
         tile_cells = self.tile_cells
         pipe_tries = 0
         while True:
-            reorder = TILED_REORDER if (want_tiles and self.reorder == "rcm") else self.reorder
-            self.layout_order = reorder if want_tiles else self.reorder
+            # self.reorder "rcm": renumbering allowed (the layout picks the order)
+            reorder = self.reorder if self.reorder != "rcm" else (TILED_REORDER if want_tiles else STAGED_REORDER)
+            self.layout_order = reorder
             # the tiled layout of a CUDA engine is built on the GPU (partition,
             # slots, rings); RCM numberings are a host pass
             on_gpu = self.device.type == "cuda" and reorder != "rcm" and LAYOUT_ON_DEVICE
@@ -510,7 +516,7 @@ class SweEngine:
     def describe(self) -> str:
         s = (f"nc={self.nc} width={self.width} dtype={str(self.dtype).replace('torch.', '')} "
              f"kernel={'tiled' if self.tiled else 'staged'} precision={self.precision} "
-             f"reorder={self.reorder if not self.tiled else ('rcm+tiles' if self.layout_order == 'rcm' else 'tiles')}")
+             f"reorder={self.layout_order if not self.tiled else ('rcm+tiles' if self.layout_order == 'rcm' else 'tiles')}")
         if self.tiled:
             st = self.tile_stats
             s += (f" tiles={st['ntiles']} own<={st['max_own']} L3/own={st['l3_over_own']:.3f}"
@@ -977,7 +983,7 @@ def try_install(m, modules: List, mode: Optional[str] = None, precision: Optiona
         if binding is None:
             return None
         logger.info(f"{type(m).__name__}: shallow-water roles found from its structure")
-    reorder = "none" if _shared_with_others(m, modules) else "rcm"
+    reorder = "none" if _shared_with_others(m, modules) else "rcm"  # "none": no renumbering allowed
     if reorder == "none" and mode == "auto":
         mode = "staged"
     try:

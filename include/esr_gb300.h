@@ -408,21 +408,22 @@ int esr_swe_host_step(void *plan, double dt, float *host_state, int64_t steps,
 int esr_swe_host_plan_destroy(void *plan);
 
 /* Host: partition an undirected graph (directed edge lists) into parts of at
- * most max_part vertices by recursive BFS bisection (compact parts; a set
- * due to end as k = ceil(size / max_part) parts is split floor(k/2) : ceil(k/2),
- * so there are ceil(n / max_part) parts of nearly equal size for a
- * connected graph); part[v] in [0, *nparts).  No reference counterpart. */
+ * most max_part vertices by recursive BFS bisection: a set is ordered by
+ * (BFS distance from the vertex farthest from its first vertex -- largest
+ * distance, then smallest id --, id), unreached vertices last by id, and a
+ * set due to end as k = ceil(size / max_part) parts keeps its first
+ * size * floor(k/2) / k vertices on the left; ceil(n / max_part) compact
+ * parts of nearly equal size, numbered depth first; part[v] in
+ * [0, *nparts).  No reference counterpart. */
 int esr_bisect_partition(int64_t n, int64_t m, const int64_t *src,
                          const int64_t *dst, int64_t max_part, int64_t *part,
                          int64_t *nparts);
 
-/* Device: the same partition contract on the GPU (src, dst, part device
- * arrays; n and 2m below 2^31).  The same part sizes in the same order as
- * esr_bisect_partition; the parts themselves are cut from BFS distances
- * with ties broken by vertex id, so they are deterministic but not the host
- * function's.  Workspace of esr_bisect_device_workspace_bytes(n, m,
- * max_part) bytes (-1: sizes out of range).  Reads one 4-byte error count
- * back (synchronises the stream once).  No reference counterpart. */
+/* Device: the same partition on the GPU, vertex for vertex (src, dst, part
+ * device arrays; n and 2m below 2^31).  Workspace of
+ * esr_bisect_device_workspace_bytes(n, m, max_part) bytes (-1: sizes out of
+ * range).  Reads the error count and the largest degree back (synchronises
+ * the stream once).  No reference counterpart. */
 int64_t esr_bisect_device_workspace_bytes(int64_t n, int64_t m,
                                           int64_t max_part);
 int esr_bisect_partition_device(int64_t n, int64_t m, const int64_t *src,
