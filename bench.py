@@ -387,8 +387,10 @@ def bench_swe(args, world, rank, local):
         "engine": eng.describe(),
         "setup_s": {"mesh_geometry_and_module": t_mesh,
                     "compile": t_compile,
-                    "compile_note": "layout on the host: BFS-bisection tiles, tile/halo lists; and the "
-                                    "compile-time check of one fused step against the module's own forward"},
+                    "compile_note": "the first compile in the process (CUDA modules load on first use): tiled "
+                                    "layout built on the GPU (BFS-bisection partition kernels, device sorts for "
+                                    "slots and halo rings) and the compile-time check of one fused step against "
+                                    "the module's own forward"},
         "parity": ("bitwise equal to the reference CPU backend" if args.precision == "exact" else
                    "state within 1e-5 (FP32) relative max-norm of the FP64 oracle (N=100 x 1,000 steps, N=2000 x 5 "
                    "steps)"),
@@ -396,7 +398,8 @@ def bench_swe(args, world, rank, local):
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": lps * args.steps, "clocks": clk.summary(),
     }
     if not args.no_solvers:
-        del eqn, eng, host, stage, a, b
+        eng._free_host_plan()
+        del eqn, eng, host
         torch.cuda.empty_cache()
         line["secondary"]["solvers"] = solver_secondaries(args, world, rank, local)
     return line

@@ -33,6 +33,7 @@ Data layout (world size 1):
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 from typing import List, Optional
 
@@ -500,11 +501,18 @@ class SweEngine:
 
     def _free_host_plan(self) -> None:
         if getattr(self, "_host_plan", None) is not None:
-            try:
-                _lib.call("esr_swe_host_plan_destroy", self._host_plan[1])
-            except Exception:  # interpreter shutdown
-                pass
+            _destroy_host_plan(self._host_plan[1])
         self._host_plan = None
+        _drain_host_plans()
+
+    def __del__(self):
+        # the destroy synchronises the plan's copy streams, which must not
+        # happen while some stream is being captured into a CUDA graph: the
+        # collector queues the plan for the next safe point instead
+        plan = getattr(self, "_host_plan", None)
+        if plan is not None:
+            _PENDING_HOST_PLANS.append(plan[1])
+            self._host_plan = None
 
     def launches_per_step(self) -> int:
         return 1 if self.tiled else 4
@@ -571,6 +579,24 @@ class SweEngine:
     def traffic_key(self) -> str:
         """Key of this kernel variant's measured DRAM bytes per launch."""
         return f"swe_tiled_{self.tile_kernel_name()}_{self.precision}"
+
+
+_PENDING_HOST_PLANS: list = []  # host-stepping plans of collected engines
+
+
+def _destroy_host_plan(handle) -> None:
+    try:
+        _lib.call("esr_swe_host_plan_destroy", handle)
+    except Exception:  # interpreter shutdown
+        pass
+
+
+def _drain_host_plans() -> None:
+    while _PENDING_HOST_PLANS:
+        _destroy_host_plan(_PENDING_HOST_PLANS.pop())
+
+
+atexit.register(_drain_host_plans)
 
 
 def _to(a, dev) -> torch.Tensor:
