@@ -375,7 +375,8 @@ def bench_swe(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": kernel_bytes / (step_s / lps) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": kernel_bytes / (step_s / lps) / 1e9 / peak, "peak_kind": peak_kind,
                      "traffic": traffic,
-                     "kernel": ("swe_tile_step_kernel (1 launch per step)" if eng.tiled else
+                     "kernel": ((("swe_tile_pipe_kernel" if eng.tile_kernel_name().startswith("pipelined") else
+                                  "swe_tile_step_kernel") + " (1 launch per step)") if eng.tiled else
                                 "swe_stage_kernel (4 launches per step; bytes and time per step / 4)"),
                      "algorithmic_bytes_per_launch": kernel_bytes,
                      "bytes_model": eng.bytes_model(),
