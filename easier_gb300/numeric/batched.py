@@ -400,17 +400,10 @@ class BatchedPCG:
                 table.append({"tiles_per_chunk": m, "ctas_per_sm": c, "ms_per_iter": best,
                               "units_per_cta": self.nchunks / self.grid})
         self.x.copy_(x_keep)
-        # the timing has every instance running; once most have finished,
-        # a shape with few work units per CTA leaves CTAs idle: shapes with
-        # at least two chunks per persistent CTA are preferred (measured on
-        # the 256-instance batch: 32 tiles a chunk, 2.6 chunks a CTA, 1.30 s
-        # a solve; 64 tiles, 1.3 a CTA, 1.37-1.39 s, though its all-running
-        # iteration times the same), then the finest shape within 2% of the
-        # fastest of those
-        pool = [r for r in table if r["units_per_cta"] >= 2.0] or table
-        best = min(r["ms_per_iter"] for r in pool)
-        win = min((r for r in pool if r["ms_per_iter"] <= 1.02 * best),
-                  key=lambda r: (r["tiles_per_chunk"], r["ms_per_iter"]))
+        # (the timing has every instance running; rules that favour finer
+        # chunks for the tail of a batch cost more on single systems than
+        # they gain on batches: the fastest shape wins)
+        win = min(table, key=lambda r: r["ms_per_iter"])
         res = {"tiles_per_chunk": win["tiles_per_chunk"], "grid": win["ctas_per_sm"] * self.sm_count,
                "ms_per_iter": win["ms_per_iter"], "table": table}
         _TUNE_CACHE[key] = res
