@@ -275,6 +275,7 @@ class SweEngine:
         nc = b["nc"]
         sel = b["selectors"]
         idx = [sel[k].idx for k in ("gather_src", "gather_dst", "gather_b")]
+        ph = self.setup_phases = _Phases(self.device)
         want_tiles = self.mode in ("tiled", "auto") and self.dtype == torch.float32
         tiles = None
         tile_cells = self.tile_cells
@@ -290,9 +291,11 @@ class SweEngine:
                                [a.cpu().numpy().astype(np.int64) for a in idx])
             lay = cell_layout(nc, src, dst, bcell, reorder=reorder,
                               tile_cells=tile_cells if want_tiles else None)
+            ph.mark("partition_and_slots")
             if lay["part"] is None:
                 break
             tiles = tile_layout(lay["nbr"], lay["part"])
+            ph.mark("tile_lists")
             if self.precision == "fast" and reorder != "rcm":
                 # a few over-wide tiles: cut them rather than shrink every tile
                 for _ in range(2):
@@ -303,6 +306,7 @@ class SweEngine:
                         break
                     lay = cell_layout(nc, src, dst, bcell, reorder=reorder, part=split)
                     tiles = tile_layout(lay["nbr"], lay["part"])
+                    ph.mark("wide_tile_split")
             st = tiles["stats"]
             if st["max_own"] <= TILE_CELLS and st["max_l3"] <= TILE_MAX_L3 and st["smem"] <= TILE_SMEM:
                 # fast arithmetic: smaller tiles until the pipelined kernel takes them
@@ -327,12 +331,15 @@ class SweEngine:
         self.tiled = tiled
         if tiled:
             self._build_tiles(tiles)
+        ph.mark("record_order")
         self._fill_geometry()
+        ph.mark("geometry_records")
         nbuf = 2 if tiled else 1
         self.bufs = [torch.zeros((nc, 4), dtype=self.dtype, device=self.device) for _ in range(nbuf)]
         self.cur = 0
         self._pack_state()
         self.ws = None if tiled else torch.empty(3 * 4 * nc, dtype=self.dtype, device=self.device)
+        ph.mark("state_buffers")
 
     def _build_tiles(self, lay: dict) -> None:
         st = lay["stats"]
@@ -597,6 +604,29 @@ def _drain_host_plans() -> None:
 
 
 atexit.register(_drain_host_plans)
+
+
+class _Phases:
+    """Wall time of the setup phases (the device synchronised at each
+    boundary, so asynchronous work is charged to its own phase)."""
+
+    def __init__(self, device):
+        import time
+        self._time = time.perf_counter
+        self._dev = device if device.type == "cuda" else None
+        self.times = {}
+        self._sync()
+        self._t = self._time()
+
+    def _sync(self):
+        if self._dev is not None:
+            torch.cuda.synchronize(self._dev)
+
+    def mark(self, name: str) -> None:
+        self._sync()
+        t = self._time()
+        self.times[name] = self.times.get(name, 0.0) + (t - self._t)
+        self._t = t
 
 
 def _to(a, dev) -> torch.Tensor:
@@ -1017,7 +1047,9 @@ def try_install(m, modules: List, mode: Optional[str] = None, precision: Optiona
     except NotImplementedError as e:
         logger.info(f"{type(m).__name__}: not fused ({e})")
         return None
-    if not _verify(m, eng, binding):
+    ok = _verify(m, eng, binding)
+    eng.setup_phases.mark("compile_time_check")
+    if not ok:
         # undo the renumbering of the bound tensors
         for k in ("h", "uh", "vh", "area"):
             v = binding["tensors"][k]

@@ -155,3 +155,34 @@ def test_sell_layout_keeps_row_order():
         assert all(c[slice_ptr[s] + 32 * k + lane] == col[perm[rowptr[r] + k]] for k in range(len(got)))
     with pytest.raises(ValueError):
         mesh.sell_layout(n, rowptr, perm, np.full(400, n), n)
+
+
+def test_device_entry_points_check_their_arguments_first():
+    """The host-stepping plan and the device partition refuse bad arguments
+    before any CUDA call (dummy device pointers: run only where no GPU could
+    be reached)."""
+    import ctypes
+    import pytest
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("dummy device pointers: host-only check")
+    lib = _lib.lib()
+    d = 0x1000
+    tiles = _lib.SweTiles(1000, 1, _lib.F32, 900, 800, 700, 100, d, d, d, d, d, d, d, 0, 1)
+    plan = ctypes.c_void_p()
+    e = d + 0x100
+    for args, msg in (((d, e, None, d, 8), b"staging"), ((d, e, d, d, 0), b"chunks"), ((d, e, d, d, 65), b"chunks"),
+                      ((d, d + 8, d, d, 8), b"aligned"), ((d, d, d, d, 8), b"distinct")):
+        a, b_, stage, tl, ch = args
+        rc = lib.esr_swe_host_plan_create(ctypes.byref(tiles), a, b_, stage, tl, ch, ctypes.byref(plan))
+        assert rc == 1, (args, rc)
+        assert msg in lib.esr_last_error(), (args, lib.esr_last_error())
+    assert lib.esr_swe_host_step(None, 1e-3, d, 1, None) == 1
+    assert lib.esr_bisect_device_workspace_bytes(0, 10, 5) == -1
+    assert lib.esr_bisect_device_workspace_bytes(10, 10, 0) == -1
+    assert lib.esr_bisect_device_workspace_bytes(1 << 31, 10, 5) == -1
+    np_ = ctypes.c_int64()
+    assert lib.esr_bisect_partition_device(0, 0, d, d, 5, d, ctypes.byref(np_), d, 1 << 20, None) == 1
+    assert lib.esr_bisect_partition_device(10, 5, None, d, 5, d, ctypes.byref(np_), d, 1 << 20, None) == 1
+    assert lib.esr_bisect_partition_device(10, 5, d, d, 5, d, ctypes.byref(np_), d, 16, None) == 1
+    assert b"workspace too small" in lib.esr_last_error()
