@@ -30,6 +30,23 @@ def test_device_partition_equals_the_host_partition(n, max_part):
     assert np.array_equal(dp.cpu().numpy(), hp)
 
 
+def test_device_partition_of_a_high_degree_graph():
+    """Degrees above 8 take the CSR rows instead of the fixed-width ones: a
+    mesh plus hub vertices joined to many cells, and duplicate edges."""
+    nc, src, dst = _graph(40)
+    rng = np.random.default_rng(5)
+    hubs = rng.integers(0, nc, 6)
+    extra_s = np.repeat(hubs, 25)
+    extra_d = rng.integers(0, nc, extra_s.size)
+    src2 = np.concatenate([src, extra_s, src[:50]])
+    dst2 = np.concatenate([dst, extra_d, dst[:50]])
+    for max_part in (97, 640):
+        hp, hn = mesh.bisect_partition(nc, src2, dst2, max_part)
+        dp, dn = mesh.bisect_partition(nc, torch.from_numpy(src2).cuda(), torch.from_numpy(dst2).cuda(), max_part)
+        assert dn == hn
+        assert np.array_equal(dp.cpu().numpy(), hp)
+
+
 def test_device_partition_of_a_disconnected_graph():
     """Two copies of a mesh side by side (no edge between them)."""
     nc, src, dst = _graph(24)
