@@ -268,7 +268,7 @@ def test_fast_record_order_sorts_each_cells_slots():
         assert np.all(np.diff(lnbr[got], axis=0) >= 0)
 
 
-@pytest.mark.parametrize("n,tile", [(3, 8), (12, 100), (40, 700), (64, 1900)])
+@pytest.mark.parametrize("n,tile", [(3, 8), (12, 100), (40, 700), (64, 1900), (3, 1000), (1, 5)])
 def test_device_layout_functions_match_the_host_ones(n, tile):
     """The torch layout path a CUDA engine runs on the GPU (cell slots, tile
     rings, record order, slot_info), run here on CPU tensors with the host
