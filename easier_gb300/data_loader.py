@@ -12,6 +12,7 @@ from __future__ import annotations
 import copy
 from typing import Optional, Tuple, Union
 
+import numpy as np
 import torch
 
 from .utils import EasierJitException
@@ -129,11 +130,13 @@ class H5DataLoader(DataLoaderBase):
         with h5py.File(file, "r", **h5_file_kwargs) as f:
             d = f[dataset]
             self.shape = tuple(d.shape)
-            raw = torch.from_numpy(d[:0]).dtype if d.shape else torch.from_numpy(d[()]).dtype
+            # (h5py gives a NumPy scalar, not an array, for a scalar dataset)
+            raw = torch.from_numpy(np.asarray(d[:0] if d.shape else d[()])).dtype
         self.dtype = dtype if dtype is not None else raw
         self.device = torch.device(device)
 
     def _materialise(self) -> torch.Tensor:
         import h5py
         with h5py.File(self._file, "r", **self._kw) as f:
-            return torch.from_numpy(f[self._dataset][...])
+            d = f[self._dataset]
+            return torch.from_numpy(np.array(d[...] if d.shape else d[()]))
